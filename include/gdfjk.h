@@ -1,0 +1,112 @@
+/*
+ * gdfjk.h — C ABI of the GB300 density-fitted J/K engine (libgdfjk.so).
+ *
+ * The engine replaces the JK half of psi4's in-core DF path: MemDFJK::compute_JK
+ * (psi4/src/psi4/libfock/MemDFJK.cc:97-111) -> DFHelper::build_JK / compute_JK /
+ * compute_J_symm / compute_K (psi4/src/psi4/lib3index/dfhelper.cc:3015-3377).  The
+ * metric-contracted 3-index tensor B[Q][mn] = sum_P J^-1/2_QP (P|mn) is built on the
+ * host (as DFHelper::prepare_AO_core does, dfhelper.cc:514-588), uploaded to HBM once,
+ * and every Fock build then runs on the GPU.
+ *
+ * Conventions: row-major FP64 host/device matrices; every call returns an int status
+ * (GDFJK_OK = 0, negative on error) and gdfjk_last_error(h) gives the message (h may be
+ * NULL for errors before a handle exists).  One CUDA stream per handle; calls that take
+ * host buffers are synchronous, calls with the _device suffix are asynchronous on the
+ * handle's stream.  A handle is not re-entrant (like psi4's JK objects, jk.h:232).
+ */
+#ifndef GDFJK_H
+#define GDFJK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gdfjk_s* gdfjk_t;
+
+enum {
+    GDFJK_OK = 0,
+    GDFJK_ERR_ARG = -1,      /* invalid argument (sizes, null pointers, layout)        */
+    GDFJK_ERR_CUDA = -2,     /* CUDA runtime/driver error                              */
+    GDFJK_ERR_OOM = -3,      /* device allocation refused                              */
+    GDFJK_ERR_STATE = -4,    /* call out of order (e.g. compute before upload_B)       */
+    GDFJK_ERR_TIMEOUT = -5,  /* the stream did not finish within the host watchdog     */
+    GDFJK_ERR_NUMERIC = -6,  /* non-finite values found in J or K                      */
+    GDFJK_ERR_DEVICE = -7    /* a kernel reported an internal error through its flag   */
+};
+
+/* B layouts accepted by gdfjk_upload_B */
+enum {
+    GDFJK_LAYOUT_PQQ = 0,  /* DFHelper in-core pQq: B[big_skips[m] + Q*small_skips[m] + fun_index[m*nbf+n]-1]
+                              (dfhelper.cc:1671-1673); needs big_skips/small_skips/fun_index     */
+    GDFJK_LAYOUT_QTRI = 1  /* Q-major packed lower triangle: B[Q*nbf(nbf+1)/2 + m(m+1)/2 + n], m >= n */
+};
+
+/* compute mode bits */
+enum {
+    GDFJK_DO_J = 1,
+    GDFJK_DO_K = 2,
+    GDFJK_MIXED = 4,       /* K as a split-BF16 tensor-core product with FP32 accumulation      */
+    GDFJK_INCREMENTAL = 8, /* K += K(dD) against the previous build's density (mixed form only)  */
+    GDFJK_RESET = 16       /* forget the incremental history (next build is a full build)      */
+};
+
+/* Create an engine on CUDA device `device` for nbf basis functions and naux fitting
+ * functions.  pair_mask (nbf*nbf bytes, symmetric, nullable = every pair significant)
+ * is DFHelper's Schwarz function mask (schwarz_fun_index_ != 0, dfhelper.cc:375-386). */
+int gdfjk_create(int device, int nbf, int naux, const unsigned char* pair_mask, int flags, gdfjk_t* out);
+
+/* Upload B from host memory, once (MemDFJK::preiterations -> DFHelper::initialize,
+ * MemDFJK.cc:71-96).  For GDFJK_LAYOUT_PQQ pass big_skips (nbf+1), small_skips (nbf+1)
+ * and fun_index (nbf*nbf) exactly as DFHelper::prepare_sparsity builds them
+ * (dfhelper.cc:368-397); for GDFJK_LAYOUT_QTRI pass NULL for all three. */
+int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_skips, const int64_t* small_skips,
+                   const int64_t* fun_index);
+
+/* Same with B already on the device (Q-major packed lower triangle, naux*nbf(nbf+1)/2). */
+int gdfjk_upload_B_device(gdfjk_t h, const double* B_qtri_device);
+
+/* One Fock build, host buffers (JK::compute, jk.cc:595-681, for one density):
+ *   C_left  nbf x nocc (row-major, leading dimension ldc >= nocc)
+ *   C_right nbf x nocc or NULL (NULL = lr-symmetric: D = C_left C_left^T, jk.cc:597-599)
+ *   D_out   nbf x nbf or NULL: receives D = C_left C_right^T (JK::compute_D, jk.cc:314-354)
+ *   J, K    nbf x nbf outputs (overwritten, like MemDFJK::compute_JK's zero() + build)
+ * nocc = 0 gives K = 0 (dfhelper.cc:3355).  mode: GDFJK_DO_J | GDFJK_DO_K [| GDFJK_MIXED ...] */
+int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode, double* D_out,
+                  double* J, double* K);
+
+/* Same with device buffers, asynchronous on the handle's stream. */
+int gdfjk_compute_device(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode,
+                         double* D_out, double* J, double* K);
+
+/* Reverse-mode derivative of one lr-symmetric build (the differentiation form):
+ * given upstream gradients gJ = dE/dJ and gK = dE/dK (nbf x nbf, device or host per
+ * `on_device`), returns
+ *   dC     (nbf x nocc)  dE/dC_left through D = C C^T (J) and K = sum_Q (B_Q C)(B_Q C)^T,
+ *   Gamma  (naux x nbf(nbf+1)/2, Q-major packed, off-diagonal entries carry both (mn),(nm))
+ *          dE/dB_Q,mn, the 3-index density contracted later with derivative integrals.
+ * Either output may be NULL.  (Q|mi) is recomputed, not stored. */
+int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* gJ, const double* gK, double* dC,
+                   double* Gamma, int on_device);
+
+/* Device bytes the engine needs for these sizes (feeds JK::memory_estimate, jk.h:398). */
+int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes);
+
+/* Timing of the last build in milliseconds (J passes, K half-transform, K contraction). */
+int gdfjk_last_timings(gdfjk_t h, double* j_ms, double* k_transform_ms, double* k_contract_ms);
+
+/* Host watchdog: wait for the stream at most timeout_s seconds (GDFJK_ERR_TIMEOUT after). */
+int gdfjk_synchronize(gdfjk_t h, double timeout_s);
+
+/* The CUDA stream of the handle (cudaStream_t as void*). */
+void* gdfjk_stream(gdfjk_t h);
+
+int gdfjk_destroy(gdfjk_t h);
+const char* gdfjk_last_error(gdfjk_t h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,190 @@
+"""ORACLE — CPU restatement of psi4's in-core density-fitted J/K build (test infrastructure).
+
+This module is the checker for the GB300 engine.  Only ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` use it; the product never imports it.
+
+It restates, loop for loop over DFHelper's pQq layout, with numpy standing in for the BLAS
+calls:
+
+* ``JK::compute_D``                    psi4/src/psi4/libfock/jk.cc:314-354   (D = C_left C_right^T)
+* ``DFHelper::compute_J_symm``         psi4/src/psi4/lib3index/dfhelper.cc:3162-3223
+* ``DFHelper::compute_J``              psi4/src/psi4/lib3index/dfhelper.cc:3230-3285 (lr non-symmetric)
+* ``DFHelper::first_transform_pQq``    psi4/src/psi4/lib3index/dfhelper.cc:2162-2186
+* ``DFHelper::compute_K``              psi4/src/psi4/lib3index/dfhelper.cc:3350-3377
+* ``MemDFJK::compute_JK``              psi4/src/psi4/libfock/MemDFJK.cc:97-111 (zero, then build)
+
+Parity pin: psi4 itself cannot be built here (libint2 is not vendored), so this oracle is
+pinned through the reference's own golden energies (tests/scf2, tests/scf5,
+tests/pytests/test_comprehensive_jk_screening.py) and gradient (tests/scf6), reached by
+running the RHF driver with this JK on integrals from the host provider; see
+tests/test_golden.py.  It is also cross-checked against an independent dense
+einsum formulation (tests/test_oracle.py).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def compute_D(C_left, C_right=None):
+    """jk.cc:351 — D = C_left C_right^T (DGEMM 'N','T')."""
+    C_right = C_left if C_right is None else C_right
+    if C_left.shape[1] == 0:
+        return np.zeros((C_left.shape[0], C_right.shape[0]))
+    return C_left @ C_right.T
+
+
+def compute_J_symm(Ppq, sp, D, nbf, naux):
+    """dfhelper.cc:3162-3223 for one density, the whole aux range as one block (bcount=0,
+    block_size=naux, AO_core).  Returns J (nbf x nbf)."""
+    T1 = np.zeros(naux)
+    # pass 1: (Qm)(m) -> (Q), rows k, m >= k significant, off-diagonal weight 2
+    for k in range(nbf):
+        si = int(sp.small_skips[k])
+        mi = int(sp.symm_small_skips[k])
+        skip = int(sp.symm_ignored_columns[k])
+        jump = int(sp.big_skips[k])
+        if mi == 0:
+            continue
+        ms = [m for m in range(k, nbf) if sp.fun_index[k, m]]
+        Dbuf = np.array([D[k, m] if m == k else 2.0 * D[k, m] for m in ms])
+        blk = Ppq[jump: jump + naux * si].reshape(naux, si)[:, skip: skip + mi]
+        T1 += blk @ Dbuf
+    # pass 2: J_km = sum_Q B[k][Q][m] d_Q over the m >= k part, then unpack + symmetrise
+    J = np.zeros((nbf, nbf))
+    for k in range(nbf):
+        si = int(sp.small_skips[k])
+        mi = int(sp.symm_small_skips[k])
+        skip = int(sp.symm_ignored_columns[k])
+        jump = int(sp.big_skips[k])
+        if mi == 0:
+            continue
+        blk = Ppq[jump: jump + naux * si].reshape(naux, si)[:, skip: skip + mi]
+        T2 = T1 @ blk
+        ms = [m for m in range(k, nbf) if sp.fun_index[k, m]]
+        for c, m in enumerate(ms):
+            if m == k:
+                J[k, k] += T2[c]
+            else:
+                J[k, m] += T2[c]
+                J[m, k] += T2[c]
+    return J
+
+
+def compute_J(Ppq, sp, D, nbf, naux):
+    """dfhelper.cc:3230-3285: the non-symmetric J (full rows of significant n)."""
+    T1 = np.zeros(naux)
+    for k in range(nbf):
+        si = int(sp.small_skips[k])
+        if si == 0:
+            continue
+        ms = [m for m in range(nbf) if sp.fun_index[k, m]]
+        blk = Ppq[int(sp.big_skips[k]): int(sp.big_skips[k]) + naux * si].reshape(naux, si)
+        T1 += blk @ D[k, ms]
+    J = np.zeros((nbf, nbf))
+    for k in range(nbf):
+        si = int(sp.small_skips[k])
+        if si == 0:
+            continue
+        ms = [m for m in range(nbf) if sp.fun_index[k, m]]
+        blk = Ppq[int(sp.big_skips[k]): int(sp.big_skips[k]) + naux * si].reshape(naux, si)
+        J[k, ms] += T1 @ blk
+    return J
+
+
+def first_transform_pQq(Ppq, sp, Cmat, nbf, naux):
+    """dfhelper.cc:2162-2186: T[k][Q][i] = sum_{m in sig(k)} B[k][Q][m] C[m][i]."""
+    nocc = Cmat.shape[1]
+    T = np.zeros((nbf, naux, nocc))
+    for k in range(nbf):
+        si = int(sp.small_skips[k])
+        if si == 0:
+            continue
+        ms = [m for m in range(nbf) if sp.fun_index[k, m]]
+        blk = Ppq[int(sp.big_skips[k]): int(sp.big_skips[k]) + naux * si].reshape(naux, si)
+        T[k] = blk @ Cmat[ms, :]
+    return T
+
+
+def compute_K(Ppq, sp, C_left, C_right, nbf, naux, lr_symmetric=True):
+    """dfhelper.cc:3350-3377: K += T1 T2^T with inner dimension nocc*naux; nocc=0 skips."""
+    nocc = C_left.shape[1]
+    K = np.zeros((nbf, nbf))
+    if nocc == 0:
+        return K
+    T1 = first_transform_pQq(Ppq, sp, C_left, nbf, naux).reshape(nbf, naux * nocc)
+    T2 = T1 if lr_symmetric else first_transform_pQq(Ppq, sp, C_right, nbf, naux).reshape(nbf, naux * nocc)
+    K += T1 @ T2.T
+    return K
+
+
+class OracleJK:
+    """psi4.core.JK-shaped front end over the restatement (MemDFJK semantics)."""
+
+    def __init__(self, Ppq, sparsity, nbf, naux):
+        self.Ppq = np.asarray(Ppq, dtype=np.float64)
+        self.sp = sparsity
+        self.nbf, self.naux = nbf, naux
+        self.do_J = True
+        self.do_K = True
+        self._Cl, self._Cr = [], []
+        self._J, self._K, self._D = [], [], []
+
+    def name(self):
+        return "OracleMemDFJK"
+
+    def initialize(self):
+        pass
+
+    def set_do_J(self, v):
+        self.do_J = bool(v)
+
+    def set_do_K(self, v):
+        self.do_K = bool(v)
+
+    def C_clear(self):
+        self._Cl, self._Cr = [], []
+
+    def C_left_add(self, C):
+        self._Cl.append(np.asarray(C, dtype=np.float64))
+
+    def C_right_add(self, C):
+        self._Cr.append(np.asarray(C, dtype=np.float64))
+
+    def C_add(self, C):
+        self.C_left_add(C)
+        self.C_right_add(C)
+
+    def compute(self):
+        lr_symmetric = len(self._Cr) == 0  # jk.cc:597-599
+        Cr = self._Cl if lr_symmetric else self._Cr
+        self._D = [compute_D(l, r) for l, r in zip(self._Cl, Cr)]
+        self._J, self._K = [], []
+        for l, r, D in zip(self._Cl, Cr, self._D):
+            if self.do_J:
+                Jf = compute_J_symm if lr_symmetric else compute_J
+                self._J.append(Jf(self.Ppq, self.sp, D, self.nbf, self.naux))
+            if self.do_K:
+                self._K.append(compute_K(self.Ppq, self.sp, l, r, self.nbf, self.naux, lr_symmetric))
+
+    def J(self):
+        return self._J
+
+    def K(self):
+        return self._K
+
+    def D(self):
+        return self._D
+
+
+def dense_jk(B_dense, D, C_left=None, C_right=None):
+    """Independent dense formulation used to cross-check the loop restatement:
+    J_mn = sum_Q B_Qmn (sum_ls B_Qls D_ls), K_mn = sum_Q (B_Q C_l)(B_Q C_r)^T."""
+    d = np.einsum("qls,ls->q", B_dense, D)
+    J = np.einsum("qmn,q->mn", B_dense, d)
+    K = None
+    if C_left is not None:
+        C_right = C_left if C_right is None else C_right
+        Xl = np.einsum("qmn,ni->qmi", B_dense, C_left)
+        Xr = np.einsum("qmn,ni->qmi", B_dense, C_right)
+        K = np.einsum("qmi,qni->mn", Xl, Xr)
+    return J, K

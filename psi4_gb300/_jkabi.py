@@ -1,0 +1,48 @@
+"""ctypes signatures of libgdfjk.so (include/gdfjk.h)."""
+import ctypes
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+D = ctypes.c_double
+SZ = ctypes.c_size_t
+
+# name -> (restype, argtypes); the list is the whole exported C ABI of include/gdfjk.h
+SIGNATURES = {
+    "gdfjk_create": (I, [I, I, I, P, I, ctypes.POINTER(P)]),
+    "gdfjk_upload_B": (I, [P, P, I, P, P, P]),
+    "gdfjk_upload_B_device": (I, [P, P]),
+    "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
+    "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
+    "gdfjk_backward": (I, [P, P, I, I, P, P, P, P, I]),
+    "gdfjk_query_memory": (I, [I, I, I, I, ctypes.POINTER(SZ)]),
+    "gdfjk_last_timings": (I, [P, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(D)]),
+    "gdfjk_synchronize": (I, [P, D]),
+    "gdfjk_stream": (P, [P]),
+    "gdfjk_destroy": (I, [P]),
+    "gdfjk_last_error": (ctypes.c_char_p, [P]),
+}
+
+GDFJK_OK = 0
+GDFJK_ERR_ARG = -1
+GDFJK_ERR_CUDA = -2
+GDFJK_ERR_OOM = -3
+GDFJK_ERR_STATE = -4
+GDFJK_ERR_TIMEOUT = -5
+GDFJK_ERR_NUMERIC = -6
+GDFJK_ERR_DEVICE = -7
+
+LAYOUT_PQQ = 0
+LAYOUT_QTRI = 1
+
+DO_J = 1
+DO_K = 2
+MIXED = 4
+INCREMENTAL = 8
+RESET = 16
+
+
+def declare(L):
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args

@@ -1,0 +1,76 @@
+// common.cuh — shared definitions of the GB300 DF-JK engine.
+//
+// Device layout of B (the metric-contracted 3-index tensor B[Q][m][n], symmetric in mn):
+// the nbf x nbf matrix of every Q is cut into 64 x 64 tiles; only tiles (I, J) with I >= J
+// that hold at least one Schwarz-significant pair are stored ("stored tiles"), each as a
+// dense row-major 64 x 64 block (screened pairs and padding are zero).  Diagonal tiles are
+// stored in full (both triangles).  Storage is Q-major:
+//     B[((size_t)Q * ntiles + t) * 4096 + r * 64 + c] = B_Q[64*I_t + r][64*J_t + c].
+// This keeps every tile a contiguous 32 KB block (bulk copies, coalesced streaming) and
+// the whole of one Q contiguous; an upper-triangle tile is read as the transpose of its
+// stored mirror.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace gdfjk {
+
+constexpr int TILE = 64;
+constexpr int TILE_ELEMS = TILE * TILE;
+
+// device-side error codes written into the handle's flag word (never __trap)
+constexpr int DEV_ERR_INDEX = 1;
+constexpr int DEV_ERR_WAIT = 2;
+
+struct TileLayout {
+    int nT;          // tiles per dimension
+    int ntiles;      // stored tiles
+    const int* tI;   // [ntiles]
+    const int* tJ;   // [ntiles]
+    const int* map;  // [nT*nT]: stored index of (I, J) for I >= J, -1 if absent
+};
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace gdfjk
+
+// kernels (defined in j_kernels.cu / k_fp64.cu); all enqueue on `stream`.
+namespace gdfjk {
+
+void launch_relayout_qtri(const double* src, int q0, int nq, int nbf, const TileLayout& L, double* B,
+                          cudaStream_t stream);
+void launch_pad_C(const double* C, int nbf, int nocc, int ldc, int nbf_pad, int nocc_pad, double* Cpad,
+                  cudaStream_t stream);
+void launch_density(const double* Cl, const double* Cr, int nbf_pad, int nocc_pad, double* D, cudaStream_t stream);
+void launch_weighted_density_tiles(const double* D, int nbf_pad, const TileLayout& L, double* Dw, cudaStream_t stream);
+void launch_j_pass1(const double* B, const double* Dw, int naux, const TileLayout& L, double* dq, cudaStream_t stream);
+void launch_j_pass2(const double* B, const double* dq, int naux, const TileLayout& L, double* Jt, cudaStream_t stream);
+void launch_unpack_tiles(const double* Xt, const TileLayout& L, int nbf, int nbf_pad, double* out, int ld,
+                         bool symmetric, cudaStream_t stream);
+void launch_k_transform_fp64(const double* B, const double* Cpad, int naux, int nbf_pad, int nocc_pad,
+                             const TileLayout& L, double* X, cudaStream_t stream);
+void launch_k_contract_fp64(const double* Xl, const double* Xr, int nbf_pad, size_t kdim, bool symmetric,
+                            const TileLayout& L, double* Kpart, int nsplit, double* Kt, cudaStream_t stream);
+// sum_Q B_Q Y_Q with Y[n][Q][i] (row stride naux*nocc_pad): partial[qblock][m][i]
+int back_transform_qblocks(int naux);
+void launch_back_transform_fp64(const double* B, const double* Y, int naux, int nbf_pad, int nocc_pad,
+                                const TileLayout& L, double* partial, cudaStream_t stream);
+int k_contract_splits(int nbf_pad, size_t kdim, bool symmetric);
+void launch_unpack_lower_full(const double* Xt, int nT, int nbf, double* out, int ld, cudaStream_t stream);
+void launch_copy_out(const double* src, int nbf, int nbf_pad, double* dst, cudaStream_t stream);
+// backward.cu
+void launch_pad_sym(const double* g, int nbf, int nbf_pad, double* out, cudaStream_t stream);
+void launch_gemm_nn_fp64(int M, size_t N, int K, const double* A, size_t lda, const double* Bm, size_t ldb, double alpha,
+                         double beta, double* out, size_t ldo, cudaStream_t stream);
+void launch_gamma(const double* Y, const double* C, const double* gJ, const double* D, const double* dq,
+                  const double* gq, int naux, int nbf, int nbf_pad, int nocc_pad, const TileLayout& L, double* out,
+                  cudaStream_t stream);
+void launch_reduce_blocks(const double* part, int nblk, size_t n, double alpha, double beta, double* out,
+                          cudaStream_t stream);
+void launch_copy_rect(const double* src, int nbf, int nocc, int nocc_pad, double* dst, int ldd, cudaStream_t stream);
+void launch_finite_check(const double* a, size_t n, int* flag, cudaStream_t stream);
+
+}  // namespace gdfjk

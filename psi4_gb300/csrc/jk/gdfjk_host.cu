@@ -1,0 +1,609 @@
+// gdfjk_host.cu — host side of the GB300 DF-JK engine and its C ABI (include/gdfjk.h).
+//
+// One handle = one device, one CUDA stream, B resident in HBM in the tiled layout of
+// common.cuh, and workspaces sized on first use.  A Fock build (gdfjk_compute) follows
+// JK::compute (psi4/src/psi4/libfock/jk.cc:595-681) for one density:
+//   compute_D (jk.cc:314-354)  ->  MemDFJK::compute_JK (MemDFJK.cc:97-111):
+//   zero J/K, then DFHelper::compute_J_symm / compute_K (dfhelper.cc:3162-3377)
+// with the J passes and the K kernels on the GPU.  Errors become status codes with a
+// message (psi4 throws PSIEXCEPTION at the same places: jk.cc:607-634 for mismatched
+// C_left/C_right, dfhelper.cc:167-173 for memory).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gdfjk.h"
+#include "common.cuh"
+#include "mixed.cuh"
+
+using namespace gdfjk;
+
+namespace {
+thread_local std::string g_create_err;
+}
+
+struct gdfjk_s {
+    int device = 0;
+    int nbf = 0, naux = 0, nT = 0, nbf_pad = 0, ntiles = 0;
+    int flags = 0;
+    std::vector<int> tI, tJ, map;
+    cudaStream_t stream = nullptr;
+    int *d_tI = nullptr, *d_tJ = nullptr, *d_map = nullptr;
+    int* d_err = nullptr;  // device-side error flag word
+    double* B = nullptr;   // naux * ntiles * 4096
+    bool B_ready = false;
+    // workspaces
+    int cap_nocc = -1;
+    double *Cl = nullptr, *Cr = nullptr, *D = nullptr, *Dw = nullptr, *dq = nullptr, *Jt = nullptr;
+    double *Xl = nullptr, *Xr = nullptr, *Kpart = nullptr, *Kt = nullptr;
+    size_t Kpart_elems = 0;
+    double *dJ = nullptr, *dK = nullptr, *dD = nullptr, *dCin = nullptr, *dCrin = nullptr;  // host-path staging
+    size_t dCin_elems = 0;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    float t_j = 0, t_kt = 0, t_kc = 0;
+    MixedState* mixed = nullptr;
+    // backward workspaces
+    double *gJp = nullptr, *gKp = nullptr, *Jg = nullptr, *Yb = nullptr, *Zpart = nullptr, *dCp = nullptr;
+    double *gq = nullptr, *Dw2 = nullptr, *Jgt = nullptr, *hC = nullptr, *hgJ = nullptr, *hgK = nullptr, *hdC = nullptr,
+           *hG = nullptr;
+    int bw_cap_nocc = -1;
+    std::string err;
+};
+
+namespace {
+
+int set_err(gdfjk_t h, int code, const std::string& msg) {
+    if (h)
+        h->err = msg;
+    else
+        g_create_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) {                                                                     \
+            return set_err(h, e_ == cudaErrorMemoryAllocation ? GDFJK_ERR_OOM : GDFJK_ERR_CUDA,      \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+        }                                                                                            \
+    } while (0)
+
+template <class T>
+int dalloc(gdfjk_t h, T** p, size_t n) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (n == 0) return GDFJK_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        char buf[160];
+        snprintf(buf, sizeof buf, "device allocation of %.3f GB refused (%s)", n * sizeof(T) / 1e9,
+                 cudaGetErrorString(e));
+        return set_err(h, e == cudaErrorMemoryAllocation ? GDFJK_ERR_OOM : GDFJK_ERR_CUDA, buf);
+    }
+    return GDFJK_OK;
+}
+
+TileLayout layout_of(gdfjk_t h) { return TileLayout{h->nT, h->ntiles, h->d_tI, h->d_tJ, h->d_map}; }
+
+int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym) {
+    int rc;
+    size_t np2 = (size_t)h->nbf_pad * h->nbf_pad;
+    if (!h->D) {
+        if ((rc = dalloc(h, &h->D, np2))) return rc;
+        if ((rc = dalloc(h, &h->Dw, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+        if ((rc = dalloc(h, &h->dq, (size_t)std::max(h->naux, 1)))) return rc;
+        if ((rc = dalloc(h, &h->Jt, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+        int nout_full = h->nT * h->nT;
+        if ((rc = dalloc(h, &h->Kt, (size_t)nout_full * TILE_ELEMS))) return rc;
+    }
+    if (nocc_pad > h->cap_nocc || (nonsym && !h->Xr && nocc_pad > 0)) {
+        int cap = std::max(nocc_pad, h->cap_nocc);
+        size_t xe = (size_t)h->nbf_pad * h->naux * cap;
+        if ((rc = dalloc(h, &h->Cl, (size_t)h->nbf_pad * std::max(cap, 1)))) return rc;
+        if ((rc = dalloc(h, &h->Cr, (size_t)h->nbf_pad * std::max(cap, 1)))) return rc;
+        if ((rc = dalloc(h, &h->Xl, xe))) return rc;
+        if (nonsym || h->Xr) {
+            if ((rc = dalloc(h, &h->Xr, xe))) return rc;
+        }
+        h->cap_nocc = cap;
+    }
+    // split-K partials
+    size_t kdim = (size_t)h->naux * std::max(nocc_pad, 1);
+    int ns = k_contract_splits(h->nbf_pad, kdim, !nonsym);
+    int nout = nonsym ? h->nT * h->nT : h->nT * (h->nT + 1) / 2;
+    size_t need = (size_t)ns * nout * TILE_ELEMS;
+    if (need > h->Kpart_elems) {
+        if ((rc = dalloc(h, &h->Kpart, need))) return rc;
+        h->Kpart_elems = need;
+    }
+    return GDFJK_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Enqueue one build on the handle's stream; all pointers are device pointers.
+int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode, double* D_out,
+                  double* J, double* K) {
+    const bool do_J = mode & GDFJK_DO_J;
+    const bool do_K = mode & GDFJK_DO_K;
+    const bool nonsym = C_right != nullptr;
+    const int nocc_pad = round_up(std::max(nocc, 0), 32);
+    int rc = ensure_workspace(h, nocc_pad, nonsym);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    TileLayout L = layout_of(h);
+    CK(cudaEventRecord(h->ev[0], s));
+    // C (padded to nbf_pad x nocc_pad) and D = C_left C_right^T
+    if (nocc_pad > 0) {
+        launch_pad_C(C_left, h->nbf, nocc, ldc, h->nbf_pad, nocc_pad, h->Cl, s);
+        if (nonsym) launch_pad_C(C_right, h->nbf, nocc, ldc, h->nbf_pad, nocc_pad, h->Cr, s);
+    }
+    launch_density(h->Cl, nonsym ? h->Cr : h->Cl, h->nbf_pad, nocc_pad, h->D, s);
+    if (D_out) launch_copy_out(h->D, h->nbf, h->nbf_pad, D_out, s);
+    if (do_J) {
+        launch_weighted_density_tiles(h->D, h->nbf_pad, L, h->Dw, s);
+        launch_j_pass1(h->B, h->Dw, h->naux, L, h->dq, s);
+        launch_j_pass2(h->B, h->dq, h->naux, L, h->Jt, s);
+        launch_unpack_tiles(h->Jt, L, h->nbf, h->nbf_pad, J, h->nbf, true, s);
+    }
+    CK(cudaEventRecord(h->ev[1], s));
+    CK(cudaEventRecord(h->ev[2], s));
+    if (do_K) {
+        if (nocc == 0) {
+            CK(cudaMemsetAsync(K, 0, sizeof(double) * (size_t)h->nbf * h->nbf, s));
+            CK(cudaEventRecord(h->ev[3], s));
+        } else if (mode & GDFJK_MIXED) {
+            if (nonsym) return set_err(h, GDFJK_ERR_ARG, "mixed-precision K needs an lr-symmetric density");
+            rc = mixed_build_K(h->mixed, h->B, L, h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
+                               h->ev[3], s, h->err);
+            if (rc) return rc;
+        } else {
+            launch_k_transform_fp64(h->B, h->Cl, h->naux, h->nbf_pad, nocc_pad, L, h->Xl, s);
+            if (nonsym) launch_k_transform_fp64(h->B, h->Cr, h->naux, h->nbf_pad, nocc_pad, L, h->Xr, s);
+            CK(cudaEventRecord(h->ev[3], s));
+            size_t kdim = (size_t)h->naux * nocc_pad;
+            int ns = k_contract_splits(h->nbf_pad, kdim, !nonsym);
+            launch_k_contract_fp64(h->Xl, nonsym ? h->Xr : h->Xl, h->nbf_pad, kdim, !nonsym, L, h->Kpart, ns, h->Kt, s);
+            if (nonsym)
+                launch_unpack_tiles(h->Kt, L, h->nbf, h->nbf_pad, K, h->nbf, false, s);
+            else
+                launch_unpack_lower_full(h->Kt, h->nT, h->nbf, K, h->nbf, s);
+        }
+    } else {
+        CK(cudaEventRecord(h->ev[3], s));
+    }
+    CK(cudaEventRecord(h->ev[4], s));
+    CK(cudaGetLastError());
+    return GDFJK_OK;
+}
+
+int wait_stream(gdfjk_t h, double timeout_s) {
+    auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaStreamQuery(h->stream);
+        if (e == cudaSuccess) return GDFJK_OK;
+        if (e != cudaErrorNotReady) return set_err(h, GDFJK_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_s > 0 && el > timeout_s) {
+            char buf[128];
+            snprintf(buf, sizeof buf, "stream did not finish within %.1f s", timeout_s);
+            return set_err(h, GDFJK_ERR_TIMEOUT, buf);
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(el < 0.01 ? 20 : 500));
+    }
+}
+
+int check_device_flag(gdfjk_t h) {
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (flag) {
+        CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+        if (flag & 4) return set_err(h, GDFJK_ERR_NUMERIC, "non-finite values in J or K");
+        return set_err(h, GDFJK_ERR_DEVICE, "a kernel reported an internal error (flag " + std::to_string(flag) + ")");
+    }
+    return GDFJK_OK;
+}
+
+double env_timeout() {
+    const char* s = getenv("GDFJK_TIMEOUT_S");
+    return s ? atof(s) : 600.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gdfjk_last_error(gdfjk_t h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes) {
+    if (nbf <= 0 || naux <= 0 || max_nocc < 0 || !bytes) return set_err(nullptr, GDFJK_ERR_ARG, "query_memory: bad sizes");
+    int nT = (nbf + TILE - 1) / TILE;
+    size_t nbf_pad = (size_t)nT * TILE;
+    size_t ntiles = (size_t)nT * (nT + 1) / 2;  // upper bound (no screening)
+    size_t nocc_pad = (size_t)round_up(max_nocc, 32);
+    size_t b = (size_t)naux * ntiles * TILE_ELEMS * 8;          // B
+    b += nbf_pad * nbf_pad * 8 + 2 * ntiles * TILE_ELEMS * 8;    // D, Dw, Jt
+    b += (size_t)nT * nT * TILE_ELEMS * 8 + naux * 8;            // Kt, dq
+    b += nbf_pad * naux * nocc_pad * 8;                          // X
+    b += 2 * nbf_pad * nocc_pad * 8;                             // C
+    int ns = k_contract_splits((int)nbf_pad, (size_t)naux * std::max<size_t>(nocc_pad, 1), true);
+    b += (size_t)ns * ntiles * TILE_ELEMS * 8;                   // split-K partials
+    if (flags & GDFJK_MIXED) b += mixed_query_memory(nbf, naux, max_nocc);
+    *bytes = b;
+    return GDFJK_OK;
+}
+
+int gdfjk_create(int device, int nbf, int naux, const unsigned char* pair_mask, int flags, gdfjk_t* out) {
+    if (!out) return set_err(nullptr, GDFJK_ERR_ARG, "create: out is NULL");
+    *out = nullptr;
+    if (nbf <= 0 || naux <= 0) return set_err(nullptr, GDFJK_ERR_ARG, "create: nbf and naux must be positive");
+    if (naux > 65535) return set_err(nullptr, GDFJK_ERR_ARG, "create: naux above 65535 is not supported");
+    gdfjk_t h = new gdfjk_s();
+    h->device = device;
+    h->nbf = nbf;
+    h->naux = naux;
+    h->flags = flags;
+    h->nT = (nbf + TILE - 1) / TILE;
+    h->nbf_pad = h->nT * TILE;
+    // tile list: (I, J), I >= J, holding at least one significant pair
+    h->map.assign((size_t)h->nT * h->nT, -1);
+    for (int I = 0; I < h->nT; ++I)
+        for (int J = 0; J <= I; ++J) {
+            bool any = false;
+            if (!pair_mask) {
+                any = true;
+            } else {
+                for (int r = 0; r < TILE && !any; ++r)
+                    for (int c = 0; c < TILE && !any; ++c) {
+                        int m = I * TILE + r, n = J * TILE + c;
+                        if (m < nbf && n < nbf && pair_mask[(size_t)m * nbf + n]) any = true;
+                    }
+            }
+            if (any) {
+                h->map[(size_t)I * h->nT + J] = (int)h->tI.size();
+                h->tI.push_back(I);
+                h->tJ.push_back(J);
+            }
+        }
+    h->ntiles = (int)h->tI.size();
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        std::string m = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        delete h;
+        return set_err(nullptr, GDFJK_ERR_CUDA, m);
+    }
+    int rc = GDFJK_OK;
+    auto fail = [&](int code) {
+        g_create_err = h->err;
+        gdfjk_destroy(h);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        h->err = "cudaStreamCreate failed";
+        return fail(GDFJK_ERR_CUDA);
+    }
+    for (auto& ev : h->ev)
+        if (cudaEventCreate(&ev) != cudaSuccess) {
+            h->err = "cudaEventCreate failed";
+            return fail(GDFJK_ERR_CUDA);
+        }
+    if ((rc = dalloc(h, &h->d_tI, std::max<size_t>(h->ntiles, 1)))) return fail(rc);
+    if ((rc = dalloc(h, &h->d_tJ, std::max<size_t>(h->ntiles, 1)))) return fail(rc);
+    if ((rc = dalloc(h, &h->d_map, h->map.size()))) return fail(rc);
+    if ((rc = dalloc(h, &h->d_err, 1))) return fail(rc);
+    if (h->ntiles) {
+        cudaMemcpy(h->d_tI, h->tI.data(), sizeof(int) * h->ntiles, cudaMemcpyHostToDevice);
+        cudaMemcpy(h->d_tJ, h->tJ.data(), sizeof(int) * h->ntiles, cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy(h->d_map, h->map.data(), sizeof(int) * h->map.size(), cudaMemcpyHostToDevice);
+    cudaMemset(h->d_err, 0, sizeof(int));
+    h->mixed = mixed_create();
+    if (cudaGetLastError() != cudaSuccess) {
+        h->err = "create: CUDA error while initialising";
+        return fail(GDFJK_ERR_CUDA);
+    }
+    *out = h;
+    return GDFJK_OK;
+}
+
+int gdfjk_destroy(gdfjk_t h) {
+    if (!h) return GDFJK_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    double* bufs[] = {h->B,   h->Cl,  h->Cr,  h->D,     h->Dw,  h->dq,  h->Jt,  h->Xl, h->Xr,  h->Kpart,
+                      h->Kt,  h->dJ,  h->dK,  h->dD,    h->dCin, h->dCrin, h->gJp, h->gKp, h->Jg, h->Yb,
+                      h->Zpart, h->dCp, h->gq, h->Dw2, h->Jgt, h->hC,  h->hgJ, h->hgK, h->hdC, h->hG};
+    for (double* p : bufs)
+        if (p) cudaFree(p);
+    if (h->d_tI) cudaFree(h->d_tI);
+    if (h->d_tJ) cudaFree(h->d_tJ);
+    if (h->d_map) cudaFree(h->d_map);
+    if (h->d_err) cudaFree(h->d_err);
+    mixed_destroy(h->mixed);
+    for (auto& ev : h->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GDFJK_OK;
+}
+
+void* gdfjk_stream(gdfjk_t h) { return h ? (void*)h->stream : nullptr; }
+
+int gdfjk_upload_B_device(gdfjk_t h, const double* Bq) {
+    if (!h || !Bq) return set_err(h, GDFJK_ERR_ARG, "upload_B_device: null argument");
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if (!h->B) {
+        if ((rc = dalloc(h, &h->B, (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+    }
+    TileLayout L = layout_of(h);
+    const int chunk = 4096;
+    size_t npair = (size_t)h->nbf * (h->nbf + 1) / 2;
+    for (int q0 = 0; q0 < h->naux; q0 += chunk) {
+        int nq = std::min(chunk, h->naux - q0);
+        launch_relayout_qtri(Bq + (size_t)q0 * npair, q0, nq, h->nbf, L, h->B, h->stream);
+    }
+    CK(cudaGetLastError());
+    if ((rc = wait_stream(h, env_timeout()))) return rc;
+    mixed_invalidate(h->mixed);
+    h->B_ready = true;
+    return GDFJK_OK;
+}
+
+int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_skips, const int64_t* small_skips,
+                   const int64_t* fun_index) {
+    if (!h || !B) return set_err(h, GDFJK_ERR_ARG, "upload_B: null argument");
+    if (layout != GDFJK_LAYOUT_PQQ && layout != GDFJK_LAYOUT_QTRI)
+        return set_err(h, GDFJK_ERR_ARG, "upload_B: unknown layout");
+    if (layout == GDFJK_LAYOUT_PQQ && (!big_skips || !small_skips || !fun_index))
+        return set_err(h, GDFJK_ERR_ARG, "upload_B: the pQq layout needs big_skips, small_skips and fun_index");
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if (!h->B) {
+        if ((rc = dalloc(h, &h->B, (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+    }
+    const size_t nbf = h->nbf;
+    const size_t npair = nbf * (nbf + 1) / 2;
+    // chunk of Q rows staged as packed triangles: about 256 MB per buffer
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>(h->naux, (256ull << 20) / (npair * 8)));
+    double* host_stage[2] = {nullptr, nullptr};
+    double* dev_stage[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    auto cleanup = [&]() {
+        for (int k = 0; k < 2; ++k) {
+            if (host_stage[k]) cudaFreeHost(host_stage[k]);
+            if (dev_stage[k]) cudaFree(dev_stage[k]);
+            if (done[k]) cudaEventDestroy(done[k]);
+        }
+    };
+    for (int k = 0; k < 2; ++k) {
+        if (cudaMallocHost(&host_stage[k], (size_t)chunk * npair * 8) != cudaSuccess ||
+            cudaMalloc(&dev_stage[k], (size_t)chunk * npair * 8) != cudaSuccess ||
+            cudaEventCreate(&done[k]) != cudaSuccess) {
+            cudaGetLastError();
+            cleanup();
+            return set_err(h, GDFJK_ERR_OOM, "upload_B: staging allocation refused");
+        }
+    }
+    TileLayout L = layout_of(h);
+    unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    int buf = 0;
+    for (int q0 = 0; q0 < h->naux; q0 += chunk, buf ^= 1) {
+        int nq = std::min(chunk, h->naux - q0);
+        cudaEventSynchronize(done[buf]);  // staging buffer free again
+        double* st = host_stage[buf];
+        // gather this chunk into packed triangles on the host
+        auto work = [&](unsigned tid) {
+            for (size_t m = tid; m < nbf; m += nth) {
+                for (int qq = 0; qq < nq; ++qq) {
+                    double* dst = st + (size_t)qq * npair + m * (m + 1) / 2;
+                    size_t Q = (size_t)(q0 + qq);
+                    if (layout == GDFJK_LAYOUT_QTRI) {
+                        std::memcpy(dst, B + Q * npair + m * (m + 1) / 2, (m + 1) * sizeof(double));
+                    } else {
+                        // pQq row m: B[big_skips[m] + Q*small_skips[m] + fun_index[m][n]-1]
+                        const double* row = B + big_skips[m] + Q * small_skips[m];
+                        const int64_t* fi = fun_index + m * nbf;
+                        for (size_t n = 0; n <= m; ++n) dst[n] = fi[n] ? row[fi[n] - 1] : 0.0;
+                    }
+                }
+            }
+        };
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nth; ++t) pool.emplace_back(work, t);
+        work(0);
+        for (auto& th : pool) th.join();
+        if (cudaMemcpyAsync(dev_stage[buf], st, (size_t)nq * npair * 8, cudaMemcpyHostToDevice, h->stream) !=
+            cudaSuccess) {
+            cleanup();
+            return set_err(h, GDFJK_ERR_CUDA, "upload_B: host-to-device copy failed");
+        }
+        launch_relayout_qtri(dev_stage[buf], q0, nq, h->nbf, L, h->B, h->stream);
+        cudaEventRecord(done[buf], h->stream);
+    }
+    cudaError_t e = cudaGetLastError();
+    rc = wait_stream(h, env_timeout());
+    cleanup();
+    if (e != cudaSuccess) return set_err(h, GDFJK_ERR_CUDA, std::string("upload_B: ") + cudaGetErrorString(e));
+    if (rc) return rc;
+    mixed_invalidate(h->mixed);
+    h->B_ready = true;
+    return GDFJK_OK;
+}
+
+int gdfjk_compute_device(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode,
+                         double* D_out, double* J, double* K) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "compute: null handle");
+    if (!h->B_ready) return set_err(h, GDFJK_ERR_STATE, "compute: B has not been uploaded (call gdfjk_upload_B first)");
+    if (nocc < 0 || (nocc > 0 && (!C_left || ldc < nocc))) return set_err(h, GDFJK_ERR_ARG, "compute: bad C / nocc / ldc");
+    if ((mode & GDFJK_DO_J) && !J) return set_err(h, GDFJK_ERR_ARG, "compute: J output is NULL");
+    if ((mode & GDFJK_DO_K) && !K) return set_err(h, GDFJK_ERR_ARG, "compute: K output is NULL");
+    CK(cudaSetDevice(h->device));
+    return enqueue_build(h, C_left, C_right, nocc, ldc, mode, D_out, J, K);
+}
+
+int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode, double* D_out,
+                  double* J, double* K) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "compute: null handle");
+    if (!h->B_ready) return set_err(h, GDFJK_ERR_STATE, "compute: B has not been uploaded (call gdfjk_upload_B first)");
+    if (nocc < 0 || (nocc > 0 && (!C_left || ldc < nocc))) return set_err(h, GDFJK_ERR_ARG, "compute: bad C / nocc / ldc");
+    if ((mode & GDFJK_DO_J) && !J) return set_err(h, GDFJK_ERR_ARG, "compute: J output is NULL");
+    if ((mode & GDFJK_DO_K) && !K) return set_err(h, GDFJK_ERR_ARG, "compute: K output is NULL");
+    CK(cudaSetDevice(h->device));
+    int rc;
+    size_t n2 = (size_t)h->nbf * h->nbf;
+    size_t cin = (size_t)h->nbf * std::max(ldc, 1);
+    if (!h->dJ) {
+        if ((rc = dalloc(h, &h->dJ, n2))) return rc;
+        if ((rc = dalloc(h, &h->dK, n2))) return rc;
+        if ((rc = dalloc(h, &h->dD, n2))) return rc;
+    }
+    if (cin > h->dCin_elems) {
+        if ((rc = dalloc(h, &h->dCin, cin))) return rc;
+        if ((rc = dalloc(h, &h->dCrin, cin))) return rc;
+        h->dCin_elems = cin;
+    }
+    cudaStream_t s = h->stream;
+    if (nocc > 0) {
+        CK(cudaMemcpyAsync(h->dCin, C_left, cin * 8, cudaMemcpyHostToDevice, s));
+        if (C_right) CK(cudaMemcpyAsync(h->dCrin, C_right, cin * 8, cudaMemcpyHostToDevice, s));
+    }
+    rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, C_right ? h->dCrin : nullptr, nocc, std::max(ldc, 1), mode,
+                       D_out ? h->dD : nullptr, h->dJ, h->dK);
+    if (rc) return rc;
+    if (mode & GDFJK_DO_J) launch_finite_check(h->dJ, n2, h->d_err, s);
+    if (mode & GDFJK_DO_K) launch_finite_check(h->dK, n2, h->d_err, s);
+    if (mode & GDFJK_DO_J) CK(cudaMemcpyAsync(J, h->dJ, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if (mode & GDFJK_DO_K) CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if (D_out) CK(cudaMemcpyAsync(D_out, h->dD, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if ((rc = wait_stream(h, env_timeout()))) return rc;
+    return check_device_flag(h);
+}
+
+int gdfjk_synchronize(gdfjk_t h, double timeout_s) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "synchronize: null handle");
+    CK(cudaSetDevice(h->device));
+    int rc = wait_stream(h, timeout_s);
+    if (rc) return rc;
+    return check_device_flag(h);
+}
+
+int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* gJ, const double* gK, double* dC,
+                   double* Gamma, int on_device) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "backward: null handle");
+    if (!h->B_ready) return set_err(h, GDFJK_ERR_STATE, "backward: B has not been uploaded");
+    if (nocc < 0 || (nocc > 0 && (!C || ldc < nocc)) || !gJ || !gK)
+        return set_err(h, GDFJK_ERR_ARG, "backward: bad C / nocc / ldc or null gradients");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const int nbf = h->nbf, nbf_pad = h->nbf_pad, naux = h->naux;
+    const int nocc_pad = round_up(std::max(nocc, 0), 32);
+    int rc = ensure_workspace(h, std::max(nocc_pad, 32), false);
+    if (rc) return rc;
+    size_t np2 = (size_t)nbf_pad * nbf_pad, n2 = (size_t)nbf * nbf;
+    size_t npair = (size_t)nbf * (nbf + 1) / 2;
+    if (!h->gJp) {
+        if ((rc = dalloc(h, &h->gJp, np2)) || (rc = dalloc(h, &h->gKp, np2)) || (rc = dalloc(h, &h->Jg, np2)) ||
+            (rc = dalloc(h, &h->gq, (size_t)naux)) || (rc = dalloc(h, &h->Dw2, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS)) ||
+            (rc = dalloc(h, &h->Jgt, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS)))
+            return rc;
+    }
+    if (nocc_pad > h->bw_cap_nocc) {
+        int nqb = back_transform_qblocks(naux);
+        if ((rc = dalloc(h, &h->Yb, (size_t)nbf_pad * naux * nocc_pad)) ||
+            (rc = dalloc(h, &h->Zpart, (size_t)nqb * nbf_pad * nocc_pad)) ||
+            (rc = dalloc(h, &h->dCp, (size_t)nbf_pad * nocc_pad)))
+            return rc;
+        h->bw_cap_nocc = nocc_pad;
+    }
+    const double *dC_in = C, *dgJ = gJ, *dgK = gK;
+    double *dC_out = dC, *dG = Gamma;
+    if (!on_device) {
+        // host-buffer path: stage through device copies sized for this call
+        if ((rc = dalloc(h, &h->hC, (size_t)nbf * std::max(ldc, 1))) || (rc = dalloc(h, &h->hgJ, n2)) ||
+            (rc = dalloc(h, &h->hgK, n2)) || (rc = dalloc(h, &h->hdC, (size_t)nbf * std::max(nocc, 1))))
+            return rc;
+        if (Gamma && (rc = dalloc(h, &h->hG, (size_t)naux * npair))) return rc;
+        if (nocc > 0) CK(cudaMemcpyAsync(h->hC, C, (size_t)nbf * ldc * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(h->hgJ, gJ, n2 * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(h->hgK, gK, n2 * 8, cudaMemcpyHostToDevice, s));
+        dC_in = h->hC;
+        dgJ = h->hgJ;
+        dgK = h->hgK;
+        dC_out = dC ? h->hdC : nullptr;
+        dG = Gamma ? h->hG : nullptr;
+    }
+    TileLayout L = layout_of(h);
+    // forward pieces: padded C, D, d_Q, X
+    if (nocc_pad > 0) launch_pad_C(dC_in, nbf, nocc, ldc, nbf_pad, nocc_pad, h->Cl, s);
+    launch_density(h->Cl, h->Cl, nbf_pad, nocc_pad, h->D, s);
+    launch_weighted_density_tiles(h->D, nbf_pad, L, h->Dw, s);
+    launch_j_pass1(h->B, h->Dw, naux, L, h->dq, s);
+    // g_Q = sum B_Q,mn gJ_mn
+    launch_pad_sym(dgJ, nbf, nbf_pad, h->gJp, s);
+    launch_pad_sym(dgK, nbf, nbf_pad, h->gKp, s);
+    launch_weighted_density_tiles(h->gJp, nbf_pad, L, h->Dw2, s);
+    launch_j_pass1(h->B, h->Dw2, naux, L, h->gq, s);
+    if (nocc_pad > 0) {
+        launch_k_transform_fp64(h->B, h->Cl, naux, nbf_pad, nocc_pad, L, h->Xl, s);
+        // Y = gK X   (X viewed as nbf_pad x (naux*nocc_pad))
+        size_t kd = (size_t)naux * nocc_pad;
+        launch_gemm_nn_fp64(nbf_pad, kd, nbf_pad, h->gKp, nbf_pad, h->Xl, kd, 1.0, 0.0, h->Yb, kd, s);
+    }
+    if (dG) {
+        CK(cudaMemsetAsync(dG, 0, (size_t)naux * npair * 8, s));
+        if (nocc_pad > 0)
+            launch_gamma(h->Yb, h->Cl, h->gJp, h->D, h->dq, h->gq, naux, nbf, nbf_pad, nocc_pad, L, dG, s);
+    }
+    if (dC_out && nocc > 0) {
+        // J[gJ] = sum_Q B_Q g_Q (dense, padded)
+        launch_j_pass2(h->B, h->gq, naux, L, h->Jgt, s);
+        CK(cudaMemsetAsync(h->Jg, 0, np2 * 8, s));
+        launch_unpack_tiles(h->Jgt, L, nbf, nbf_pad, h->Jg, nbf_pad, true, s);
+        // Z = sum_Q B_Q Y_Q  (fixed-order reduction over Q blocks), dC = 2 Z + 2 J[gJ] C
+        launch_back_transform_fp64(h->B, h->Yb, naux, nbf_pad, nocc_pad, L, h->Zpart, s);
+        int nqb = back_transform_qblocks(naux);
+        int qper = (naux + nqb - 1) / nqb;
+        nqb = (naux + qper - 1) / qper;
+        launch_reduce_blocks(h->Zpart, nqb, (size_t)nbf_pad * nocc_pad, 2.0, 0.0, h->dCp, s);
+        launch_gemm_nn_fp64(nbf_pad, nocc_pad, nbf_pad, h->Jg, nbf_pad, h->Cl, nocc_pad, 2.0, 1.0, h->dCp, nocc_pad, s);
+        launch_copy_rect(h->dCp, nbf, nocc, nocc_pad, dC_out, on_device ? ldc : nocc, s);
+    }
+    CK(cudaGetLastError());
+    if (!on_device) {
+        if (dC && nocc > 0) CK(cudaMemcpyAsync(dC, h->hdC, (size_t)nbf * nocc * 8, cudaMemcpyDeviceToHost, s));
+        if (Gamma) CK(cudaMemcpyAsync(Gamma, h->hG, (size_t)naux * npair * 8, cudaMemcpyDeviceToHost, s));
+        if ((rc = wait_stream(h, env_timeout()))) return rc;
+        return check_device_flag(h);
+    }
+    return GDFJK_OK;
+}
+
+int gdfjk_last_timings(gdfjk_t h, double* j_ms, double* kt_ms, double* kc_ms) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "last_timings: null handle");
+    float a = 0, b = 0, c = 0;
+    CK(cudaEventSynchronize(h->ev[4]));
+    CK(cudaEventElapsedTime(&a, h->ev[0], h->ev[1]));
+    CK(cudaEventElapsedTime(&b, h->ev[2], h->ev[3]));
+    CK(cudaEventElapsedTime(&c, h->ev[3], h->ev[4]));
+    if (j_ms) *j_ms = a;
+    if (kt_ms) *kt_ms = b;
+    if (kc_ms) *kc_ms = c;
+    return GDFJK_OK;
+}
+
+}  // extern "C"

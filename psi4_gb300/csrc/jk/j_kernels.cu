@@ -1,0 +1,317 @@
+// j_kernels.cu — layout, density and Coulomb (J) kernels of the GB300 DF-JK engine.
+//
+// The J build restates DFHelper::compute_J_symm (psi4/src/psi4/lib3index/dfhelper.cc:3162-3223)
+// over the tiled device layout of B (common.cuh):
+//   pass 1  d_Q  = sum_{m,n} B_Q,mn D_mn          (psi4: per-row DGEMV('N') + thread reduction)
+//   pass 2  J_mn = sum_Q     B_Q,mn d_Q           (psi4: per-row DGEMV('T') + unpack/symmetrise)
+// Both passes stream B once from HBM with 16-byte vector loads and fixed-order reductions
+// (no atomics), so results are bitwise reproducible run to run.  Off-diagonal stored tiles
+// stand for both (m,n) and (n,m): pass 1 weights them by 2 (psi4's "2 * D" for m != k).
+#include "common.cuh"
+
+namespace gdfjk {
+
+// ---------------------------------------------------------------- relayout
+// src: nq rows of the Q-major packed lower triangle, Q = q0 .. q0+nq-1.
+__global__ void relayout_qtri_kernel(const double* __restrict__ src, int q0, int nq, int nbf, int nT, int ntiles,
+                                     const int* __restrict__ tI, const int* __restrict__ tJ, double* __restrict__ B) {
+    int t = blockIdx.x;
+    int qq = blockIdx.y;
+    size_t npair = (size_t)nbf * (nbf + 1) / 2;
+    const double* row = src + (size_t)qq * npair;
+    double* dst = B + ((size_t)(q0 + qq) * ntiles + t) * TILE_ELEMS;
+    int I = tI[t], J = tJ[t];
+    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) {
+        int r = e / TILE, c = e % TILE;
+        int m = I * TILE + r, n = J * TILE + c;
+        double v = 0.0;
+        if (m < nbf && n < nbf) {
+            size_t hi = m > n ? m : n, lo = m > n ? n : m;
+            v = row[hi * (hi + 1) / 2 + lo];
+        }
+        dst[e] = v;
+    }
+}
+
+void launch_relayout_qtri(const double* src, int q0, int nq, int nbf, const TileLayout& L, double* B,
+                          cudaStream_t stream) {
+    if (nq <= 0 || L.ntiles == 0) return;
+    dim3 grid(L.ntiles, nq);
+    relayout_qtri_kernel<<<grid, 256, 0, stream>>>(src, q0, nq, nbf, L.nT, L.ntiles, L.tI, L.tJ, B);
+}
+
+// ---------------------------------------------------------------- C padding
+__global__ void pad_C_kernel(const double* __restrict__ C, int nbf, int nocc, int ldc, int nbf_pad, int nocc_pad,
+                             double* __restrict__ Cp) {
+    size_t n = (size_t)nbf_pad * nocc_pad;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        int m = (int)(e / nocc_pad), i = (int)(e % nocc_pad);
+        Cp[e] = (m < nbf && i < nocc) ? C[(size_t)m * ldc + i] : 0.0;
+    }
+}
+
+void launch_pad_C(const double* C, int nbf, int nocc, int ldc, int nbf_pad, int nocc_pad, double* Cpad,
+                  cudaStream_t stream) {
+    size_t n = (size_t)nbf_pad * nocc_pad;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    pad_C_kernel<<<blocks, 256, 0, stream>>>(C, nbf, nocc, ldc, nbf_pad, nocc_pad, Cpad);
+}
+
+// ---------------------------------------------------------------- D = Cl Cr^T (JK::compute_D, jk.cc:351)
+// 32x32 output tile per block, 16-deep k steps through shared memory.
+__global__ void density_kernel(const double* __restrict__ Cl, const double* __restrict__ Cr, int nbf_pad,
+                               int nocc_pad, double* __restrict__ D) {
+    __shared__ double As[16][33];
+    __shared__ double Bs[16][33];
+    int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 16 x 16 threads, 2x2 outputs each
+    int m0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+    double acc[2][2] = {{0, 0}, {0, 0}};
+    for (int k0 = 0; k0 < nocc_pad; k0 += 16) {
+        for (int e = threadIdx.x; e < 512; e += 256) {
+            int r = e / 16, k = e % 16;
+            As[k][r] = Cl[(size_t)(m0 + r) * nocc_pad + k0 + k];
+            Bs[k][r] = Cr[(size_t)(n0 + r) * nocc_pad + k0 + k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            double a0 = As[k][ty * 2], a1 = As[k][ty * 2 + 1];
+            double b0 = Bs[k][tx * 2], b1 = Bs[k][tx * 2 + 1];
+            acc[0][0] += a0 * b0;
+            acc[0][1] += a0 * b1;
+            acc[1][0] += a1 * b0;
+            acc[1][1] += a1 * b1;
+        }
+        __syncthreads();
+    }
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) D[(size_t)(m0 + ty * 2 + a) * nbf_pad + n0 + tx * 2 + b] = acc[a][b];
+}
+
+void launch_density(const double* Cl, const double* Cr, int nbf_pad, int nocc_pad, double* D, cudaStream_t stream) {
+    dim3 grid(nbf_pad / 32, nbf_pad / 32);
+    if (nocc_pad == 0) {
+        cudaMemsetAsync(D, 0, sizeof(double) * (size_t)nbf_pad * nbf_pad, stream);
+        return;
+    }
+    density_kernel<<<grid, 256, 0, stream>>>(Cl, Cr, nbf_pad, nocc_pad, D);
+}
+
+// Dw[t][r][c] = w_t * (D_mn + D_nm)/2, w_t = 1 on diagonal tiles, 2 off the diagonal.
+__global__ void weighted_density_kernel(const double* __restrict__ D, int nbf_pad, const int* __restrict__ tI,
+                                        const int* __restrict__ tJ, double* __restrict__ Dw) {
+    int t = blockIdx.x;
+    int I = tI[t], J = tJ[t];
+    double w = (I == J) ? 0.5 : 1.0;
+    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) {
+        int r = e / TILE, c = e % TILE;
+        size_t m = (size_t)I * TILE + r, n = (size_t)J * TILE + c;
+        Dw[(size_t)t * TILE_ELEMS + e] = w * (D[m * nbf_pad + n] + D[n * nbf_pad + m]);
+    }
+}
+
+void launch_weighted_density_tiles(const double* D, int nbf_pad, const TileLayout& L, double* Dw, cudaStream_t stream) {
+    if (L.ntiles == 0) return;
+    weighted_density_kernel<<<L.ntiles, 256, 0, stream>>>(D, nbf_pad, L.tI, L.tJ, Dw);
+}
+
+// ---------------------------------------------------------------- block reduction helper
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x / 32, l = threadIdx.x % 32;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < (int)(blockDim.x / 32); ++k) s += sh[k];
+    }
+    return s;
+}
+
+// ---------------------------------------------------------------- J pass 1: d_Q
+// One block per Q; the block streams B_Q (ntiles*4096 doubles, contiguous) once with
+// 16-byte loads, four independent partial sums per thread; Dw stays L2 resident.
+constexpr int JP1_THREADS = 512;
+__global__ void __launch_bounds__(JP1_THREADS) j_pass1_kernel(const double* __restrict__ B,
+                                                              const double* __restrict__ Dw, size_t per_q,
+                                                              double* __restrict__ dq) {
+    __shared__ double sh[JP1_THREADS / 32];
+    int Q = blockIdx.x;
+    const double2* b = reinterpret_cast<const double2*>(B + (size_t)Q * per_q);
+    const double2* w = reinterpret_cast<const double2*>(Dw);
+    size_t n2 = per_q / 2;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    size_t i = threadIdx.x;
+    const size_t step = JP1_THREADS;
+    for (; i + 3 * step < n2; i += 4 * step) {
+        double2 x0 = __ldcs(b + i), x1 = __ldcs(b + i + step), x2 = __ldcs(b + i + 2 * step), x3 = __ldcs(b + i + 3 * step);
+        double2 y0 = __ldg(w + i), y1 = __ldg(w + i + step), y2 = __ldg(w + i + 2 * step), y3 = __ldg(w + i + 3 * step);
+        a0 = fma(x0.x, y0.x, fma(x0.y, y0.y, a0));
+        a1 = fma(x1.x, y1.x, fma(x1.y, y1.y, a1));
+        a2 = fma(x2.x, y2.x, fma(x2.y, y2.y, a2));
+        a3 = fma(x3.x, y3.x, fma(x3.y, y3.y, a3));
+    }
+    for (; i < n2; i += step) {
+        double2 x0 = __ldcs(b + i), y0 = __ldg(w + i);
+        a0 = fma(x0.x, y0.x, fma(x0.y, y0.y, a0));
+    }
+    double s = block_sum((a0 + a1) + (a2 + a3), sh);
+    if (threadIdx.x == 0) dq[Q] = s;
+}
+
+void launch_j_pass1(const double* B, const double* Dw, int naux, const TileLayout& L, double* dq, cudaStream_t stream) {
+    if (naux == 0) return;
+    size_t per_q = (size_t)L.ntiles * TILE_ELEMS;
+    if (per_q == 0) {
+        cudaMemsetAsync(dq, 0, sizeof(double) * naux, stream);
+        return;
+    }
+    j_pass1_kernel<<<naux, JP1_THREADS, 0, stream>>>(B, Dw, per_q, dq);
+}
+
+// ---------------------------------------------------------------- J pass 2: J tiles
+// Each block owns 1024 consecutive tile elements (2 double2 per thread) and sweeps all Q,
+// taking d_Q from shared memory in chunks; fixed Q order per element.
+constexpr int JP2_THREADS = 256;
+constexpr int JP2_DCHUNK = 2048;
+__global__ void __launch_bounds__(JP2_THREADS) j_pass2_kernel(const double* __restrict__ B,
+                                                              const double* __restrict__ dq, int naux, size_t per_q,
+                                                              double* __restrict__ Jt) {
+    __shared__ double ds[JP2_DCHUNK];
+    size_t base2 = (size_t)blockIdx.x * (2 * JP2_THREADS) + threadIdx.x;  // double2 index
+    size_t n2 = per_q / 2;
+    const double2* b = reinterpret_cast<const double2*>(B);
+    size_t qstride = n2;
+    bool ok0 = base2 < n2, ok1 = base2 + JP2_THREADS < n2;
+    double2 acc0 = make_double2(0, 0), acc1 = make_double2(0, 0);
+    for (int q0 = 0; q0 < naux; q0 += JP2_DCHUNK) {
+        int nq = min(JP2_DCHUNK, naux - q0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < nq; k += JP2_THREADS) ds[k] = dq[q0 + k];
+        __syncthreads();
+        const double2* bq = b + (size_t)q0 * qstride + base2;
+        int q = 0;
+        for (; q + 3 < nq; q += 4) {
+            double d0 = ds[q], d1 = ds[q + 1], d2 = ds[q + 2], d3 = ds[q + 3];
+            double2 x0 = ok0 ? __ldcs(bq) : make_double2(0, 0);
+            double2 x1 = ok0 ? __ldcs(bq + qstride) : make_double2(0, 0);
+            double2 x2 = ok0 ? __ldcs(bq + 2 * qstride) : make_double2(0, 0);
+            double2 x3 = ok0 ? __ldcs(bq + 3 * qstride) : make_double2(0, 0);
+            double2 y0 = ok1 ? __ldcs(bq + JP2_THREADS) : make_double2(0, 0);
+            double2 y1 = ok1 ? __ldcs(bq + qstride + JP2_THREADS) : make_double2(0, 0);
+            double2 y2 = ok1 ? __ldcs(bq + 2 * qstride + JP2_THREADS) : make_double2(0, 0);
+            double2 y3 = ok1 ? __ldcs(bq + 3 * qstride + JP2_THREADS) : make_double2(0, 0);
+            acc0.x = fma(d3, x3.x, fma(d2, x2.x, fma(d1, x1.x, fma(d0, x0.x, acc0.x))));
+            acc0.y = fma(d3, x3.y, fma(d2, x2.y, fma(d1, x1.y, fma(d0, x0.y, acc0.y))));
+            acc1.x = fma(d3, y3.x, fma(d2, y2.x, fma(d1, y1.x, fma(d0, y0.x, acc1.x))));
+            acc1.y = fma(d3, y3.y, fma(d2, y2.y, fma(d1, y1.y, fma(d0, y0.y, acc1.y))));
+            bq += 4 * qstride;
+        }
+        for (; q < nq; ++q) {
+            double d0 = ds[q];
+            if (ok0) {
+                double2 x0 = __ldcs(bq);
+                acc0.x = fma(d0, x0.x, acc0.x);
+                acc0.y = fma(d0, x0.y, acc0.y);
+            }
+            if (ok1) {
+                double2 y0 = __ldcs(bq + JP2_THREADS);
+                acc1.x = fma(d0, y0.x, acc1.x);
+                acc1.y = fma(d0, y0.y, acc1.y);
+            }
+            bq += qstride;
+        }
+    }
+    double2* out = reinterpret_cast<double2*>(Jt);
+    if (ok0) out[base2] = acc0;
+    if (ok1) out[base2 + JP2_THREADS] = acc1;
+}
+
+void launch_j_pass2(const double* B, const double* dq, int naux, const TileLayout& L, double* Jt, cudaStream_t stream) {
+    size_t per_q = (size_t)L.ntiles * TILE_ELEMS;
+    if (per_q == 0) return;
+    size_t n2 = per_q / 2;
+    int blocks = (int)((n2 + 2 * JP2_THREADS - 1) / (2 * JP2_THREADS));
+    j_pass2_kernel<<<blocks, JP2_THREADS, 0, stream>>>(B, dq, naux, per_q, Jt);
+}
+
+// ---------------------------------------------------------------- tiles -> dense nbf x nbf
+// symmetric: Xt holds the stored lower tiles (layout map); otherwise Xt holds all nT*nT
+// tiles in row-major tile order.
+__global__ void unpack_tiles_kernel(const double* __restrict__ Xt, int nT, const int* __restrict__ map, int nbf,
+                                    double* __restrict__ out, int ld, int symmetric, int full_lower) {
+    size_t n = (size_t)nbf * nbf;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        int m = (int)(e / nbf), k = (int)(e % nbf);
+        int I = m / TILE, J = k / TILE;
+        double v = 0.0;
+        if (!symmetric) {
+            v = Xt[((size_t)I * nT + J) * TILE_ELEMS + (m % TILE) * TILE + (k % TILE)];
+        } else {
+            int hi = I >= J ? I : J, lo = I >= J ? J : I;
+            int t = full_lower ? (hi * (hi + 1) / 2 + lo) : map[hi * nT + lo];
+            if (t >= 0) {
+                if (I > J || (I == J))
+                    v = Xt[(size_t)t * TILE_ELEMS + (m % TILE) * TILE + (k % TILE)];
+                else
+                    v = Xt[(size_t)t * TILE_ELEMS + (k % TILE) * TILE + (m % TILE)];
+            }
+        }
+        out[(size_t)m * ld + k] = v;
+    }
+}
+
+void launch_unpack_tiles(const double* Xt, const TileLayout& L, int nbf, int nbf_pad, double* out, int ld,
+                         bool symmetric, cudaStream_t stream) {
+    (void)nbf_pad;
+    size_t n = (size_t)nbf * nbf;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    unpack_tiles_kernel<<<blocks, 256, 0, stream>>>(Xt, L.nT, L.map, nbf, out, ld, symmetric ? 1 : 0, 0);
+}
+
+// K output tiles use the full lower-triangle enumeration t = I(I+1)/2 + J (every tile pair,
+// not only B's stored ones).
+void launch_unpack_lower_full(const double* Xt, int nT, int nbf, double* out, int ld, cudaStream_t stream) {
+    size_t n = (size_t)nbf * nbf;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    unpack_tiles_kernel<<<blocks, 256, 0, stream>>>(Xt, nT, nullptr, nbf, out, ld, 1, 1);
+}
+
+// ---------------------------------------------------------------- misc
+__global__ void copy_out_kernel(const double* __restrict__ src, int nbf, int nbf_pad, double* __restrict__ dst) {
+    size_t n = (size_t)nbf * nbf;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        int m = (int)(e / nbf), k = (int)(e % nbf);
+        dst[e] = src[(size_t)m * nbf_pad + k];
+    }
+}
+
+void launch_copy_out(const double* src, int nbf, int nbf_pad, double* dst, cudaStream_t stream) {
+    size_t n = (size_t)nbf * nbf;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    copy_out_kernel<<<blocks, 256, 0, stream>>>(src, nbf, nbf_pad, dst);
+}
+
+__global__ void finite_check_kernel(const double* __restrict__ a, size_t n, int* flag) {
+    int bad = 0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        if (!isfinite(a[e])) bad = 1;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 4);
+}
+
+void launch_finite_check(const double* a, size_t n, int* flag, cudaStream_t stream) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    finite_check_kernel<<<blocks, 256, 0, stream>>>(a, n, flag);
+}
+
+}  // namespace gdfjk

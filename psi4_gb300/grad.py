@@ -1,0 +1,66 @@
+"""RHF nuclear gradient with the density-fitted two-electron part from the GB300 engine.
+
+The engine's backward (``gdfjk_backward``) returns Gamma = dE/dB in B-space
+(B = M^-1/2 A, A = raw (P|mn), M = (P|Q)).  The host then maps it to the raw-integral
+densities psi4's DFJKGrad contracts with derivative integrals
+(psi4/src/psi4/scfgrad/jk_grad.cc:175-293, build_AB_x_terms :834-867, build_Amn_x_terms
+:868-1245):
+
+    3-index density  G3 = dE/dA = M^-1/2 Gamma
+    2-index density  G2 = dE/dM = Frechet derivative of M -> M^-1/2 applied to
+                     W = Gamma A^T (eigenbasis form, same eigenvalue truncation as the
+                     forward Matrix::power, psi4/src/psi4/libmints/matrix.cc:2370-2415)
+
+and assembles (scf_grad.cc:196-296, restricted case, alpha densities D and W):
+
+    dE/dx = E_nuc^x + 2 D.(T^x + V^x) - 2 W.S^x + G3.(A|mn)^x + G2.(P|Q)^x
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def metric_power_frechet(M, W, power=-0.5, condition=1e-10):
+    """dE/dM given dE/dF = W for F = M^power with psi4's eigenvalue truncation."""
+    w, V = np.linalg.eigh(M)
+    max_a = max(abs(w[-1]), abs(w[0]))
+    keep = np.abs(w) >= condition * max_a if power < 0 else np.ones_like(w, dtype=bool)
+    f = np.where(keep, np.abs(w) ** power, 0.0)
+    fp = np.where(keep, power * np.abs(w) ** (power - 1.0), 0.0)
+    dl = w[:, None] - w[None, :]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        Lm = (f[:, None] - f[None, :]) / dl
+    same = np.abs(dl) <= 1e-14 * np.maximum(1.0, np.abs(w[:, None]))
+    Lm = np.where(same, 0.5 * (fp[:, None] + fp[None, :]), Lm)
+    Ws = 0.5 * (W + W.T)
+    return V @ (Lm * (V.T @ Ws @ V)) @ V.T
+
+
+def two_electron_gradient(ints, df, Gamma, A_raw=None):
+    """Contract Gamma (dE/dB, packed) with derivative integrals through B = M^-1/2 A."""
+    if A_raw is None:
+        A_raw = ints.three_index(shell_mask=df.sparsity.shell_mask)
+        r, c = np.tril_indices(df.nbf)
+        A_raw[:, ~df.sparsity.pair_mask[r, c]] = 0.0
+    G3 = df.Jmhalf @ Gamma
+    W = Gamma @ A_raw.T
+    G2 = metric_power_frechet(df.metric, W)
+    g3 = ints.three_index_grad(G3, shell_mask=df.sparsity.shell_mask)
+    g2 = ints.metric_grad(G2)
+    return g3 + g2
+
+
+def rhf_gradient(mol, ints, df, scf, Gamma):
+    """Total RHF gradient (natom x 3, Eh/bohr) from a converged SCF and the engine's Gamma
+    for gJ = dE/dJ = 2D, gK = dE/dK = -D."""
+    nocc = scf.nocc
+    C = scf.C[:, :nocc]
+    eps = scf.eps[:nocc]
+    D = C @ C.T
+    W = (C * eps) @ C.T
+    g = mol.nuclear_repulsion_grad()
+    g += 2.0 * ints.kinetic_grad(D)
+    g += 2.0 * ints.potential_grad(D)
+    g -= 2.0 * ints.overlap_grad(W)
+    g += two_electron_gradient(ints, df, Gamma)
+    return g

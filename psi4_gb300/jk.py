@@ -1,0 +1,280 @@
+"""psi4.core.JK-shaped front end of the GB300 DF-JK engine.
+
+``GpuDFJK`` mirrors the JK API psi4's SCF drives (psi4/src/export_fock.cc:49-97,
+psi4/src/psi4/libfock/jk.h:232-589): ``initialize()``, ``C_left_add`` / ``C_right_add`` /
+``C_add`` / ``C_clear``, ``compute()``, ``J()``, ``K()``, ``D()``, ``memory_estimate()``,
+``print_header()``, ``set_do_J`` / ``set_do_K`` / ``set_cutoff`` / ``set_memory``.  Like
+``MemDFJK`` (psi4/src/psi4/libfock/MemDFJK.cc) it builds B = J^-1/2 (P|mn) once in
+``initialize()`` (``preiterations``) and then serves every ``compute()`` from HBM.
+
+Only lr-symmetric and non-symmetric C pairs (``C_right_add``) are served, as MemDFJK does;
+every compute goes through libgdfjk.so — there is no CPU path.  Errors raise
+``GdfjkError`` (a ``RuntimeError``, as psi4's PSIEXCEPTION surfaces in Python).
+
+Extra knobs of this engine: ``set_precision("fp64" | "mixed")`` and
+``set_incremental(True)`` (mixed form: K += K(dD) over the previous build).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _jkabi as abi
+from . import _native
+from .dfhelper import DEFAULT_CONDITION, DEFAULT_CUTOFF, DFTensor, build_df_tensor
+
+
+class GdfjkError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gdfjk error {code}: {msg}")
+        self.code = code
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class DFJKEngine:
+    """Owner of one ``gdfjk_t`` handle (one device, one stream, B resident in HBM)."""
+
+    def __init__(self, nbf: int, naux: int, pair_mask: np.ndarray | None = None, device: int = 0, flags: int = 0):
+        self.L = _native.jk_lib()
+        self.nbf, self.naux = int(nbf), int(naux)
+        h = ctypes.c_void_p()
+        self._mask = None
+        if pair_mask is not None:
+            self._mask = np.ascontiguousarray(pair_mask, dtype=np.uint8)
+            assert self._mask.shape == (nbf, nbf)
+        rc = self.L.gdfjk_create(device, self.nbf, self.naux, _p(self._mask), flags, ctypes.byref(h))
+        if rc != 0:
+            raise GdfjkError(rc, self.L.gdfjk_last_error(None).decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise GdfjkError(rc, self.L.gdfjk_last_error(self.h).decode())
+
+    # ---- B upload
+    def upload_qtri(self, B_tri: np.ndarray):
+        B = np.ascontiguousarray(B_tri, dtype=np.float64)
+        assert B.shape == (self.naux, self.nbf * (self.nbf + 1) // 2)
+        self._check(self.L.gdfjk_upload_B(self.h, _p(B), abi.LAYOUT_QTRI, None, None, None))
+
+    def upload_pqq(self, Ppq: np.ndarray, sparsity):
+        Ppq = np.ascontiguousarray(Ppq, dtype=np.float64)
+        bs = np.ascontiguousarray(sparsity.big_skips, dtype=np.int64)
+        ss = np.ascontiguousarray(sparsity.small_skips, dtype=np.int64)
+        fi = np.ascontiguousarray(sparsity.fun_index, dtype=np.int64)
+        self._check(self.L.gdfjk_upload_B(self.h, _p(Ppq), abi.LAYOUT_PQQ, _p(bs), _p(ss), _p(fi)))
+
+    def upload_device(self, ptr: int):
+        """B already in device memory as the Q-major packed triangle (e.g. a torch tensor)."""
+        self._check(self.L.gdfjk_upload_B_device(self.h, ctypes.c_void_p(ptr)))
+
+    # ---- builds
+    def compute(self, C_left, C_right=None, mode=abi.DO_J | abi.DO_K, want_D=False):
+        Cl = np.ascontiguousarray(C_left, dtype=np.float64)
+        if Cl.ndim != 2 or Cl.shape[0] != self.nbf:
+            raise GdfjkError(abi.GDFJK_ERR_ARG, f"C_left must be nbf x nocc with nbf={self.nbf}")
+        Cr = None
+        if C_right is not None:
+            Cr = np.ascontiguousarray(C_right, dtype=np.float64)
+            if Cr.shape != Cl.shape:
+                raise GdfjkError(abi.GDFJK_ERR_ARG, "JK: C_left/C_right MO zip index size mismatch!")
+        nocc = Cl.shape[1]
+        J = np.empty((self.nbf, self.nbf))
+        K = np.empty((self.nbf, self.nbf))
+        D = np.empty((self.nbf, self.nbf)) if want_D else None
+        self._check(self.L.gdfjk_compute(self.h, _p(Cl) if nocc else None, _p(Cr) if (Cr is not None and nocc) else None,
+                                         nocc, max(nocc, 1), mode, _p(D), _p(J), _p(K)))
+        return J, K, D
+
+    def compute_device(self, Cl_ptr, Cr_ptr, nocc, ldc, mode, D_ptr, J_ptr, K_ptr):
+        vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
+        self._check(self.L.gdfjk_compute_device(self.h, vp(Cl_ptr), vp(Cr_ptr), int(nocc), int(ldc), int(mode), vp(D_ptr),
+                                                vp(J_ptr), vp(K_ptr)))
+
+    def backward(self, C, gJ, gK, want_dC=True, want_gamma=True):
+        C = np.ascontiguousarray(C, dtype=np.float64)
+        nocc = C.shape[1]
+        gJ = np.ascontiguousarray(gJ, dtype=np.float64)
+        gK = np.ascontiguousarray(gK, dtype=np.float64)
+        dC = np.empty_like(C) if want_dC else None
+        G = np.empty((self.naux, self.nbf * (self.nbf + 1) // 2)) if want_gamma else None
+        self._check(self.L.gdfjk_backward(self.h, _p(C), nocc, max(nocc, 1), _p(gJ), _p(gK), _p(dC), _p(G), 0))
+        return dC, G
+
+    def backward_device(self, C_ptr, nocc, ldc, gJ_ptr, gK_ptr, dC_ptr, G_ptr):
+        vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
+        self._check(self.L.gdfjk_backward(self.h, vp(C_ptr), int(nocc), int(ldc), vp(gJ_ptr), vp(gK_ptr), vp(dC_ptr),
+                                          vp(G_ptr), 1))
+
+    def synchronize(self, timeout_s=600.0):
+        self._check(self.L.gdfjk_synchronize(self.h, float(timeout_s)))
+
+    def stream(self) -> int:
+        return int(self.L.gdfjk_stream(self.h) or 0)
+
+    def timings(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.gdfjk_last_timings(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"j_ms": a.value, "k_transform_ms": b.value, "k_contract_ms": c.value}
+
+    @staticmethod
+    def query_memory(nbf, naux, max_nocc, flags=0) -> int:
+        L = _native.jk_lib()
+        out = ctypes.c_size_t()
+        rc = L.gdfjk_query_memory(int(nbf), int(naux), int(max_nocc), int(flags), ctypes.byref(out))
+        if rc != 0:
+            raise GdfjkError(rc, L.gdfjk_last_error(None).decode())
+        return out.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gdfjk_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuDFJK:
+    """A drop-in for psi4's MemDFJK in an RHF loop, served by the GB300 engine."""
+
+    def __init__(self, primary=None, aux=None, molecule=None, df_tensor: DFTensor | None = None, device: int = 0):
+        self.primary, self.aux, self.molecule = primary, aux, molecule
+        self.df = df_tensor
+        self.device = device
+        self.cutoff = DEFAULT_CUTOFF
+        self.condition = DEFAULT_CONDITION
+        self.memory = 32_000_000  # doubles, psi4's JK default (256 MB)
+        self.do_J = True
+        self.do_K = True
+        self.precision = "fp64"
+        self.incremental = False
+        self.print_level = 1
+        self.engine: DFJKEngine | None = None
+        self._Cl, self._Cr = [], []
+        self._J, self._K, self._D = [], [], []
+        self.last_timings = {}
+
+    # psi4: core.JK.build(orbital_basis, aux, jk_type=...)
+    @staticmethod
+    def build(primary, aux, molecule, **kw) -> "GpuDFJK":
+        return GpuDFJK(primary, aux, molecule, **kw)
+
+    @staticmethod
+    def from_tensor(df: DFTensor, device: int = 0) -> "GpuDFJK":
+        return GpuDFJK(df_tensor=df, device=device)
+
+    def name(self):
+        return "GpuDFJK"
+
+    def set_do_J(self, v):
+        self.do_J = bool(v)
+
+    def set_do_K(self, v):
+        self.do_K = bool(v)
+
+    def set_cutoff(self, c):
+        self.cutoff = float(c)
+
+    def set_condition(self, c):
+        self.condition = float(c)
+
+    def set_memory(self, doubles):
+        self.memory = int(doubles)
+
+    def set_print(self, p):
+        self.print_level = int(p)
+
+    def set_precision(self, p: str):
+        if p not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = p
+
+    def set_incremental(self, v: bool):
+        self.incremental = bool(v)
+
+    def C1(self):
+        return True
+
+    def memory_estimate(self) -> int:
+        """Device bytes / 8, in doubles like psi4's JK::memory_estimate (jk.h:398)."""
+        nbf = self.df.nbf if self.df is not None else self.primary.nbf
+        naux = self.df.naux if self.df is not None else self.aux.nbf
+        flags = abi.MIXED if self.precision == "mixed" else 0
+        return DFJKEngine.query_memory(nbf, naux, nbf, flags) // 8
+
+    def initialize(self):
+        """preiterations(): build B on the host, upload it to HBM once."""
+        if self.df is None:
+            self.df = build_df_tensor(self.molecule, self.primary, self.aux, self.cutoff, self.condition)
+        df = self.df
+        self.engine = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask, device=self.device)
+        self.engine.upload_pqq(df.to_pQq(), df.sparsity)
+
+    def print_header(self):
+        if self.print_level:
+            sp = self.df.sparsity if self.df is not None else None
+            print("  ==> GpuDFJK: Density-Fitted J/K Matrices (GB300) <==\n")
+            print(f"    J tasked:           {'Yes' if self.do_J else 'No':>11s}")
+            print(f"    K tasked:           {'Yes' if self.do_K else 'No':>11s}")
+            print(f"    Precision:          {self.precision:>11s}")
+            print(f"    Schwarz Cutoff:     {self.cutoff:11.0E}")
+            if sp is not None:
+                print(f"    Mask sparsity (%):  {100.0 * sp.sparsity:11.4f}")
+            print(f"    Fitting Condition:  {self.condition:11.0E}\n")
+
+    def C_clear(self):
+        self._Cl, self._Cr = [], []
+
+    def C_left_add(self, C):
+        self._Cl.append(np.asarray(C, dtype=np.float64))
+
+    def C_right_add(self, C):
+        self._Cr.append(np.asarray(C, dtype=np.float64))
+
+    def C_add(self, C):
+        self.C_left_add(C)
+        self.C_right_add(C)
+
+    def compute(self):
+        if self.engine is None:
+            raise GdfjkError(abi.GDFJK_ERR_STATE, "JK: compute() before initialize()")
+        lr_symmetric = len(self._Cl) > 0 and len(self._Cr) == 0
+        if not lr_symmetric and len(self._Cr) != len(self._Cl):
+            raise GdfjkError(abi.GDFJK_ERR_ARG, "JK: C_left/C_right count mismatch")
+        mode = (abi.DO_J if self.do_J else 0) | (abi.DO_K if self.do_K else 0)
+        if self.precision == "mixed" and lr_symmetric:
+            mode |= abi.MIXED
+            if self.incremental:
+                mode |= abi.INCREMENTAL
+        self._J, self._K, self._D = [], [], []
+        for i, Cl in enumerate(self._Cl):
+            Cr = None if lr_symmetric else self._Cr[i]
+            if Cr is not None and Cr.shape[1] != Cl.shape[1]:
+                raise GdfjkError(abi.GDFJK_ERR_ARG, "JK: C_left/C_right MO zip index size mismatch!")
+            J, K, D = self.engine.compute(Cl, Cr, mode=mode, want_D=True)
+            self._J.append(J if self.do_J else None)
+            self._K.append(K if self.do_K else None)
+            self._D.append(D)
+        self.last_timings = self.engine.timings()
+
+    def J(self):
+        return self._J
+
+    def K(self):
+        return self._K
+
+    def D(self):
+        return self._D
+
+    def finalize(self):
+        if self.engine is not None:
+            self.engine.close()
+            self.engine = None

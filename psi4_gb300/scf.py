@@ -1,0 +1,150 @@
+"""Restricted Hartree-Fock driver around a psi4.core.JK-shaped object.
+
+This is the caller side of the DF-JK path: psi4's ``scf_iterate``
+(psi4/driver/procrouting/scf_proc/scf_iterator.py:264-609) with ``RHF::form_G`` /
+``form_F`` / ``compute_E`` / ``form_C`` / ``form_D`` (psi4/src/psi4/libscf_solver/rhf.cc:
+187-370, hf.cc:1330).  Each iteration pushes the occupied orbitals into the JK object,
+calls ``compute()`` and reads ``J()[0]``/``K()[0]``:
+
+    G = 2J - K,  F = H + G,  E = E_nuc + 2 tr(D H) + 2 tr(D J) - tr(D K)   (alpha D = C_occ C_occ^T)
+
+DIIS (Pulay, on the orthogonalised FDS - SDF, up to 10 vectors) and the diagonalisation
+stay FP64 on the host.  Convergence as ``_converged`` (scf_iterator.py:929):
+|dE| < e_conv and RMS orbital gradient < d_conv.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+class SCFConvergenceError(RuntimeError):
+    """Raised when the SCF does not converge in maxiter (scf_iterator.py:608-609)."""
+
+    def __init__(self, msg, result):
+        super().__init__(msg)
+        self.result = result
+
+
+@dataclass
+class SCFResult:
+    energy: float
+    energies: list
+    iterations: int
+    converged: bool
+    C: np.ndarray
+    eps: np.ndarray
+    D: np.ndarray
+    F: np.ndarray
+    J: np.ndarray
+    K: np.ndarray
+    nocc: int
+    timings: dict = field(default_factory=dict)
+    log: list = field(default_factory=list)
+
+
+def orthogonalizer(S, tol=1e-7):
+    """Symmetric S^-1/2, or canonical when the smallest eigenvalue is below S_TOLERANCE
+    (psi4 default 1e-7)."""
+    w, V = np.linalg.eigh(S)
+    if w.min() >= tol:
+        return (V / np.sqrt(w)) @ V.T
+    keep = w >= tol
+    return V[:, keep] / np.sqrt(w[keep])
+
+
+class DIIS:
+    def __init__(self, max_vec=10):
+        self.max_vec = max_vec
+        self.F, self.E = [], []
+
+    def add(self, F, err):
+        self.F.append(F.copy())
+        self.E.append(err.copy())
+        if len(self.F) > self.max_vec:
+            self.F.pop(0)
+            self.E.pop(0)
+
+    def extrapolate(self):
+        n = len(self.F)
+        B = -np.ones((n + 1, n + 1))
+        B[n, n] = 0.0
+        for i in range(n):
+            for j in range(i + 1):
+                B[i, j] = B[j, i] = float(np.vdot(self.E[i], self.E[j]))
+        rhs = np.zeros(n + 1)
+        rhs[n] = -1.0
+        # scale for conditioning
+        d = np.abs(np.diag(B[:n, :n])).max()
+        if d > 0:
+            B[:n, :n] /= d
+        try:
+            c = np.linalg.solve(B, rhs)[:n]
+        except np.linalg.LinAlgError:
+            c = np.linalg.lstsq(B, rhs, rcond=None)[0][:n]
+        return sum(ci * Fi for ci, Fi in zip(c, self.F))
+
+
+def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=None, diis_start=1,
+        fail_on_maxiter=True, callback=None, verbose=False) -> SCFResult:
+    """Run RHF with a JK object exposing C_clear/C_left_add/compute/J/K."""
+    X = orthogonalizer(S)
+    t0 = time.perf_counter()
+    if guess_C is None:
+        # core guess
+        eps, Cp = np.linalg.eigh(X.T @ H @ X)
+        C = X @ Cp
+    else:
+        C = guess_C
+        eps = np.zeros(C.shape[1])
+    diis = DIIS()
+    E_old = 0.0
+    energies = []
+    log = []
+    t_jk = 0.0
+    converged = False
+    it = 0
+    F = J = K = D = None
+    for it in range(1, maxiter + 1):
+        Cocc = np.ascontiguousarray(C[:, :nocc])
+        D = Cocc @ Cocc.T
+        jk.C_clear()
+        jk.C_left_add(Cocc)
+        tj = time.perf_counter()
+        jk.compute()
+        t_jk += time.perf_counter() - tj
+        J = np.asarray(jk.J()[0])
+        K = np.asarray(jk.K()[0])
+        F = H + 2.0 * J - K
+        E = e_nuc + 2.0 * np.vdot(D, H) + 2.0 * np.vdot(D, J) - np.vdot(D, K)
+        energies.append(float(E))
+        grad = X.T @ (F @ D @ S - S @ D @ F) @ X
+        dnorm = float(np.sqrt(np.mean(grad * grad)))
+        dE = E - E_old
+        log.append({"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm})
+        if verbose:
+            print(f"  @RHF iter {it:3d}: {E:20.14f} {dE: .3e} {dnorm: .3e}")
+        if callback is not None:
+            callback(it, E, dE, dnorm, D)
+        if abs(dE) < e_conv and dnorm < d_conv:
+            converged = True
+            break
+        E_old = E
+        if it >= diis_start:
+            diis.add(F, grad)
+            Fd = diis.extrapolate() if len(diis.F) >= 2 else F
+        else:
+            Fd = F
+        eps, Cp = np.linalg.eigh(X.T @ Fd @ X)
+        C = X @ Cp
+    res = SCFResult(energies[-1], energies, it, converged, C, eps, D, F, J, K, nocc,
+                    {"total_s": time.perf_counter() - t0, "jk_s": t_jk}, log)
+    if not converged and fail_on_maxiter:
+        raise SCFConvergenceError(f"Could not converge SCF iterations in {maxiter} iterations.", res)
+    return res
+
+
+def core_hamiltonian(ints):
+    return ints.kinetic() + ints.potential()

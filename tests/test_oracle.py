@@ -1,0 +1,79 @@
+"""The oracle's loop restatement of DFHelper (pQq layout) against an independent dense
+formulation, on the cases the reference's own JK tests use (tests/pytests/test_dfjk.py:
+random non-symmetric C pairs of 16-30 columns, water cc-pVDZ / cc-pVDZ-jkfit)."""
+import numpy as np
+import pytest
+
+from oracle import dfjk_ref
+from tests.helpers import random_orbitals, system
+
+
+def _dense_with_mask(df):
+    return df.dense()
+
+
+@pytest.mark.parametrize("sizes", [(16, 16), (16, 20), (20, 20), (30, 30)])
+def test_loop_restatement_matches_dense(ints_built, sizes):
+    mol, pb, ab, ints, df = system("h2o")
+    nbf, naux = df.nbf, df.naux
+    Ppq = df.to_pQq()
+    Bd = _dense_with_mask(df)
+    Cl = random_orbitals(nbf, sizes[0], 1)
+    Cr = random_orbitals(nbf, sizes[0], 2)
+    # lr-symmetric
+    D = dfjk_ref.compute_D(Cl)
+    J = dfjk_ref.compute_J_symm(Ppq, df.sparsity, D, nbf, naux)
+    K = dfjk_ref.compute_K(Ppq, df.sparsity, Cl, Cl, nbf, naux, True)
+    Jd, Kd = dfjk_ref.dense_jk(Bd, D, Cl)
+    assert np.abs(J - Jd).max() < 1e-11
+    assert np.abs(K - Kd).max() < 1e-11
+    # non-symmetric pair
+    D2 = dfjk_ref.compute_D(Cl, Cr)
+    J2 = dfjk_ref.compute_J(Ppq, df.sparsity, D2, nbf, naux)
+    K2 = dfjk_ref.compute_K(Ppq, df.sparsity, Cl, Cr, nbf, naux, False)
+    Jd2, Kd2 = dfjk_ref.dense_jk(Bd, D2, Cl, Cr)
+    assert np.abs(J2 - Jd2).max() < 1e-11
+    assert np.abs(K2 - Kd2).max() < 1e-11
+
+
+def test_screened_layout_and_jk(ints_built):
+    # two waters 9 A apart with a loose cutoff: many pairs are screened out
+    mol, pb, ab, ints, df = system("h2o_2_far", cutoff=1e-5)
+    sp = df.sparsity
+    assert 0.0 < sp.sparsity < 1.0
+    nbf, naux = df.nbf, df.naux
+    Ppq = df.to_pQq()
+    # layout formula: Ppq[big_skips[m] + Q*small_skips[m] + fun_index[m,n]-1] = B[Q,m,n]
+    rng = np.random.default_rng(0)
+    Bd = df.dense()
+    for _ in range(200):
+        m, n, Q = rng.integers(nbf), rng.integers(nbf), rng.integers(naux)
+        if sp.fun_index[m, n]:
+            idx = sp.big_skips[m] + Q * sp.small_skips[m] + sp.fun_index[m, n] - 1
+            assert Ppq[idx] == Bd[Q, m, n]
+    C = random_orbitals(nbf, 10, 4)
+    D = dfjk_ref.compute_D(C)
+    J = dfjk_ref.compute_J_symm(Ppq, sp, D, nbf, naux)
+    K = dfjk_ref.compute_K(Ppq, sp, C, C, nbf, naux, True)
+    Jd, Kd = dfjk_ref.dense_jk(Bd, D, C)
+    assert np.abs(J - Jd).max() < 1e-11
+    assert np.abs(K - Kd).max() < 1e-11
+
+
+def test_nocc_zero_skips_K(ints_built):
+    mol, pb, ab, ints, df = system("h2o")
+    C = np.zeros((df.nbf, 0))
+    K = dfjk_ref.compute_K(df.to_pQq(), df.sparsity, C, C, df.nbf, df.naux)
+    assert not K.any()
+
+
+def test_oracle_jk_object(ints_built):
+    mol, pb, ab, ints, df = system("h2o")
+    jk = dfjk_ref.OracleJK(df.to_pQq(), df.sparsity, df.nbf, df.naux)
+    C = random_orbitals(df.nbf, 5, 9)
+    jk.C_left_add(C)
+    jk.compute()
+    Jd, Kd = dfjk_ref.dense_jk(df.dense(), C @ C.T, C)
+    assert np.abs(jk.J()[0] - Jd).max() < 1e-11
+    assert np.abs(jk.K()[0] - Kd).max() < 1e-11
+    assert np.abs(jk.D()[0] - C @ C.T).max() < 1e-14
