@@ -103,6 +103,23 @@ int gdfjk_synchronize(gdfjk_t h, double timeout_s);
 /* The CUDA stream of the handle (cudaStream_t as void*). */
 void* gdfjk_stream(gdfjk_t h);
 
+/* Coulomb build that allocates nothing (no counterpart in the reference: psi4's JK objects
+ * always own their buffers).  For callers that cannot call cudaMalloc — code running under
+ * another framework's memory pool or allocator hooks, hosts that forbid allocation after
+ * start-up, drivers that fix their buffers once.  Runs on the calling thread's current
+ * device, asynchronously on `stream` (a cudaStream_t, NULL = legacy default stream):
+ *   B  device, Q-major packed lower triangle, naux x nbf(nbf+1)/2 (GDFJK_LAYOUT_QTRI)
+ *   D  device, nbf x nbf density (symmetrised internally)
+ *   J  device, nbf x nbf output, overwritten with J_mn = sum_Q B_Q,mn sum_ls B_Q,ls D_ls
+ * The fitted density d_Q is kept in a fixed file-scope device array of
+ * GDFJK_NOALLOC_MAX_NAUX doubles (512 KB) that every GPU loading the library holds until
+ * exit; naux above that limit is rejected with GDFJK_ERR_ARG.  The first call on a device
+ * resolves the array's device address (cudaGetSymbolAddress): make that first call before
+ * any stream capture.  All calls share the array and each overwrites it completely before
+ * reading it; calls whose work overlaps on the GPU race on it.  Errors: gdfjk_last_error(NULL). */
+#define GDFJK_NOALLOC_MAX_NAUX 65536
+int gdfjk_coulomb_noalloc(int nbf, int naux, const double* B, const double* D, double* J, void* stream);
+
 int gdfjk_destroy(gdfjk_t h);
 const char* gdfjk_last_error(gdfjk_t h);
 

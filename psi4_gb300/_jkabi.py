@@ -18,6 +18,7 @@ SIGNATURES = {
     "gdfjk_last_timings": (I, [P, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(D)]),
     "gdfjk_synchronize": (I, [P, D]),
     "gdfjk_stream": (P, [P]),
+    "gdfjk_coulomb_noalloc": (I, [I, I, P, P, P, P]),
     "gdfjk_destroy": (I, [P]),
     "gdfjk_last_error": (ctypes.c_char_p, [P]),
 }
@@ -39,6 +40,8 @@ DO_K = 2
 MIXED = 4
 INCREMENTAL = 8
 RESET = 16
+
+NOALLOC_MAX_NAUX = 65536
 
 
 def declare(L):

@@ -35,6 +35,9 @@ struct TileLayout {
 
 inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+// Record an error message for gdfjk_last_error(NULL) on this thread; returns `code`.
+int report_error(int code, const std::string& msg);
+
 }  // namespace gdfjk
 
 // kernels (defined in j_kernels.cu / k_fp64.cu); all enqueue on `stream`.

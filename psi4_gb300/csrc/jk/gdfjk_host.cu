@@ -29,6 +29,11 @@ namespace {
 thread_local std::string g_create_err;
 }
 
+int gdfjk::report_error(int code, const std::string& msg) {
+    g_create_err = msg;
+    return code;
+}
+
 struct gdfjk_s {
     int device = 0;
     int nbf = 0, naux = 0, nT = 0, nbf_pad = 0, ntiles = 0;
