@@ -81,6 +81,16 @@ int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int no
 int gdfjk_compute_device(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode,
                          double* D_out, double* J, double* K);
 
+/* The precision form's incremental build (psi4's INCFOCK idea, DirectJK.cc:138-166, applied
+ * to MemDFJK's exchange): J in FP64 from C (as gdfjk_compute), and
+ *   K = K_prev + sum_Q B_Q (U+ U+^T - U- U-^T) B_Q
+ * as a split-BF16 tensor-core product with FP32 accumulation, where U (nbf x nu, leading
+ * dimension ldu) holds npos positive columns then nu - npos negative ones, a signed factor
+ * of dD = D - D_prev.  K_prev is the K this handle returned last (kept on the device in
+ * FP64); GDFJK_RESET in mode takes K_prev = 0, i.e. a full build from the factor. */
+int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
+                              int mode, double* J, double* K);
+
 /* Reverse-mode derivative of one lr-symmetric build (the differentiation form):
  * given upstream gradients gJ = dE/dJ and gK = dE/dK (nbf x nbf, device or host per
  * `on_device`), returns

@@ -215,6 +215,7 @@ int check_device_flag(gdfjk_t h) {
     int flag = 0;
     CK(cudaMemcpyAsync(&flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    flag |= mixed_error_flag(h->mixed, h->stream);
     if (flag) {
         CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
         if (flag & 4) return set_err(h, GDFJK_ERR_NUMERIC, "non-finite values in J or K");
@@ -495,6 +496,53 @@ int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int no
     if (mode & GDFJK_DO_J) CK(cudaMemcpyAsync(J, h->dJ, n2 * 8, cudaMemcpyDeviceToHost, s));
     if (mode & GDFJK_DO_K) CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
     if (D_out) CK(cudaMemcpyAsync(D_out, h->dD, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if ((rc = wait_stream(h, env_timeout()))) return rc;
+    return check_device_flag(h);
+}
+
+int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
+                              int mode, double* J, double* K) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: null handle");
+    if (!h->B_ready) return set_err(h, GDFJK_ERR_STATE, "compute_incremental: B has not been uploaded");
+    if (nocc < 0 || (nocc > 0 && (!C || ldc < nocc))) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: bad C / nocc / ldc");
+    if (nu < 0 || npos < 0 || npos > nu || (nu > 0 && (!U || ldu < nu)))
+        return set_err(h, GDFJK_ERR_ARG, "compute_incremental: bad U / nu / npos / ldu");
+    if ((mode & GDFJK_DO_J) && !J) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: J output is NULL");
+    if ((mode & GDFJK_DO_K) && !K) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: K output is NULL");
+    CK(cudaSetDevice(h->device));
+    int rc;
+    size_t n2 = (size_t)h->nbf * h->nbf;
+    if (!h->dJ) {
+        if ((rc = dalloc(h, &h->dJ, n2)) || (rc = dalloc(h, &h->dK, n2)) || (rc = dalloc(h, &h->dD, n2))) return rc;
+    }
+    size_t cin = (size_t)h->nbf * std::max(ldc, 1), uin = (size_t)h->nbf * std::max(ldu, 1);
+    size_t need = std::max(cin, uin);
+    if (need > h->dCin_elems) {
+        if ((rc = dalloc(h, &h->dCin, need)) || (rc = dalloc(h, &h->dCrin, need))) return rc;
+        h->dCin_elems = need;
+    }
+    cudaStream_t s = h->stream;
+    if (nocc > 0) CK(cudaMemcpyAsync(h->dCin, C, cin * 8, cudaMemcpyHostToDevice, s));
+    if (nu > 0) CK(cudaMemcpyAsync(h->dCrin, U, uin * 8, cudaMemcpyHostToDevice, s));
+    // J (and D) in FP64 from C
+    if (mode & GDFJK_DO_J) {
+        rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_J, nullptr, h->dJ,
+                           nullptr);
+        if (rc) return rc;
+    }
+    if (mode & GDFJK_DO_K) {
+        CK(cudaEventRecord(h->ev[2], s));
+        rc = mixed_k_factor(h->mixed, h->B, layout_of(h), h->nbf, h->naux, h->dCrin, std::max(ldu, 1), npos, nu - npos,
+                            (mode & GDFJK_RESET) ? 0 : 1, h->dK, h->ev[3], s, h->err);
+        if (rc) return rc;
+        CK(cudaEventRecord(h->ev[4], s));
+        launch_finite_check(h->dK, n2, h->d_err, s);
+        CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
+    }
+    if (mode & GDFJK_DO_J) {
+        launch_finite_check(h->dJ, n2, h->d_err, s);
+        CK(cudaMemcpyAsync(J, h->dJ, n2 * 8, cudaMemcpyDeviceToHost, s));
+    }
     if ((rc = wait_stream(h, env_timeout()))) return rc;
     return check_device_flag(h);
 }

@@ -1,21 +1,557 @@
-// k_mixed.cu — split-precision exchange path (placeholder until the tcgen05 kernels land).
+// k_mixed.cu — split-precision exchange (the precision form) on the 5th-generation tensor cores.
+//
+// K = sum_Q B_Q U S U^T B_Q for a signed factor U S U^T of the density (S = +1 on the first
+// npos columns, -1 on the rest; a full build is U = C_occ, all positive; an incremental
+// build factors dD = D_new - D_old).  Two tcgen05 GEMMs with BF16 operands split in two
+// (x = x_hi + x_lo, each BF16) and FP32 accumulation in tensor memory, three products per
+// step (hi*hi + hi*lo + lo*hi, the "BF16x3" scheme of Henry, Tang & Heinecke 2019):
+//
+//   half-transform  X[(Q,m)][j] = sum_n B_Q[m][n] U[n][j]   A = B slices, rows (Q,m), K-major
+//                                                          B = U^T slices, rows j,   K-major
+//   contraction     K[m][n] = sum_{Q,j} s_j X[m][Q,j] X[n][Q,j]   lower 128x128 tiles, split-K
+//
+// The B operand of the half-transform (dense, both triangles, BF16 hi/lo) is built once from
+// the FP64 tiles.  Operand tiles arrive by TMA (64-byte swizzle, 32 k per stage) into a
+// multi-stage shared-memory ring guarded by mbarriers; one thread issues tcgen05.mma, four
+// warps drain the accumulator with tcgen05.ld.  The negative k-blocks of an incremental
+// build use the instruction's negate-A bit.  Split-K partials (FP32) are summed in FP64 in
+// a fixed order, so repeated builds are bitwise identical.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
 #include "gdfjk.h"
 #include "mixed.cuh"
+#include "tc_common.cuh"
 
 namespace gdfjk {
 
+constexpr int MM = 128;                    // tile rows (MMA M)
+constexpr int MK = 32;                     // k per pipeline stage: one 64-byte swizzle row of bf16
+constexpr int A_TILE_BYTES = MM * MK * 2;  // 8 KB
+constexpr int B_ROWS_PER_TMA = 64;
+constexpr int SMEM_BUDGET = 224 * 1024;
+constexpr int SMEM_RESERVE = 2048;         // alignment slack + barriers
+
+enum { MODE_TRANSFORM = 0, MODE_CONTRACT = 1 };
+
+struct TcArgs {
+    int nbf_p;        // padded nbf (multiple of 128)
+    int nu_pad;       // columns of U (multiple of 64)
+    int npos_pad;     // positive columns (multiple of 64)
+    int n_cols;       // accumulator columns of this launch (transform) or 128 (contraction)
+    int n_off;        // first U column of this launch (transform)
+    unsigned long long kdim;  // naux * nu_pad
+    __nv_bfloat16* Xhi;
+    __nv_bfloat16* Xlo;
+    int ntr;           // tile rows (nbf_p / 128)
+    int kb_per_split;  // 32-wide k blocks per split
+    int nkb_total;
+    int ntiles_out;
+    float* part;
+    int stages;
+    int tmem_cols;
+    int* err;
+};
+
+__device__ __forceinline__ void tile_of(int t, int& I, int& J) {
+    I = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while (I * (I + 1) / 2 > t) --I;
+    while ((I + 1) * (I + 2) / 2 <= t) ++I;
+    J = t - I * (I + 1) / 2;
+}
+
+__device__ __forceinline__ uint32_t pack_bf162(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mAh,
+                                                         const __grid_constant__ CUtensorMap mAl,
+                                                         const __grid_constant__ CUtensorMap mBh,
+                                                         const __grid_constant__ CUtensorMap mBl, const TcArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int N = a.n_cols;
+    const int b_bytes = N * MK * 2;
+    const int stage_bytes = 2 * A_TILE_BYTES + 2 * b_bytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * stage_bytes);
+    uint64_t* empty = full + a.stages;
+    uint64_t* accb = empty + a.stages;
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(accb + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+
+    const int warp = threadIdx.x / 32;
+    int a_row, b_row, kb0, nkb, tile = 0, split = 0;
+    if (MODE == MODE_TRANSFORM) {
+        a_row = blockIdx.x * MM;
+        b_row = a.n_off;
+        kb0 = 0;
+        nkb = a.nbf_p / MK;
+    } else {
+        tile = blockIdx.x;
+        split = blockIdx.y;
+        int I, J;
+        tile_of(tile, I, J);
+        a_row = I * MM;
+        b_row = J * MM;
+        kb0 = split * a.kb_per_split;
+        nkb = min(a.kb_per_split, a.nkb_total - kb0);
+    }
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < a.stages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(accb, 1);
+        *abort_flag = 0;
+        tc::fence_barrier_init();
+        tc::prefetch_tmap(&mAh);
+        tc::prefetch_tmap(&mAl);
+        tc::prefetch_tmap(&mBh);
+        tc::prefetch_tmap(&mBl);
+    }
+    if (warp == 0) tc::tmem_alloc(tmem_holder, (uint32_t)a.tmem_cols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    if (threadIdx.x == 0) {
+        // ---- TMA producer
+        for (int kb = 0; kb < nkb; ++kb) {
+            int s = kb % a.stages;
+            uint32_t ph = (uint32_t)((kb / a.stages) & 1);
+            if (kb >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) break;
+            uint8_t* st = smem + (size_t)s * stage_bytes;
+            tc::mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
+            int kx = (kb0 + kb) * MK;
+            tc::tma_load_2d(st, &mAh, &full[s], kx, a_row);
+            tc::tma_load_2d(st + A_TILE_BYTES, &mAl, &full[s], kx, a_row);
+            if (MODE == MODE_TRANSFORM) {
+                for (int r = 0; r < N; r += B_ROWS_PER_TMA) {
+                    tc::tma_load_2d(st + 2 * A_TILE_BYTES + r * MK * 2, &mBh, &full[s], kx, b_row + r);
+                    tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, &mBl, &full[s], kx, b_row + r);
+                }
+            } else {
+                tc::tma_load_2d(st + 2 * A_TILE_BYTES, &mBh, &full[s], kx, b_row);
+                tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes, &mBl, &full[s], kx, b_row);
+            }
+        }
+    } else if (threadIdx.x == 32) {
+        // ---- MMA issuer
+        for (int kb = 0; kb < nkb; ++kb) {
+            int s = kb % a.stages;
+            uint32_t ph = (uint32_t)((kb / a.stages) & 1);
+            if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) break;
+            tc::tc_fence_after();
+            uint32_t st = tc::smem_u32(smem + (size_t)s * stage_bytes);
+            uint32_t aH = st, aL = st + A_TILE_BYTES, bH = st + 2 * A_TILE_BYTES, bL = bH + b_bytes;
+            bool neg = false;
+            if (MODE == MODE_CONTRACT) {
+                unsigned long long k = (unsigned long long)(kb0 + kb) * MK;
+                neg = (int)(k % (unsigned long long)a.nu_pad) >= a.npos_pad;
+            }
+#pragma unroll
+            for (int ks = 0; ks < MK / 16; ++ks) {
+                const uint32_t koff = ks * 32;  // 16 bf16 along k
+#pragma unroll
+                for (int p = 0; p < 3; ++p) {  // hi*hi, hi*lo, lo*hi
+                    uint32_t aa = (p == 2 ? aL : aH) + koff;
+                    uint32_t bb = (p == 1 ? bL : bH) + koff;
+                    for (int nc = 0; nc < N; nc += 256) {
+                        int nn = min(256, N - nc);
+                        uint32_t acc = (kb | ks | p) != 0 ? 1u : 0u;
+                        tc::mma_bf16(tmem + (uint32_t)nc, tc::sdesc_kmajor_sw64(aa),
+                                     tc::sdesc_kmajor_sw64(bb + (uint32_t)nc * MK * 2), tc::idesc_bf16_f32(MM, nn, neg), acc);
+                    }
+                }
+            }
+            tc::mma_commit(&empty[s]);
+        }
+        tc::mma_commit(accb);
+    }
+    __syncwarp();
+
+    // ---- epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
+    bool ok = tc::mbar_wait(accb, 0, abort_flag, a.err);
+    __syncwarp();
+    tc::tc_fence_after();
+    if (ok && !*abort_flag && nkb > 0) {
+        const int r = warp * 32 + (threadIdx.x % 32);
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        if (MODE == MODE_TRANSFORM) {
+            size_t grow = (size_t)a_row + r;
+            size_t Q = grow / a.nbf_p, m = grow % a.nbf_p;
+            size_t base = m * a.kdim + Q * a.nu_pad + a.n_off;
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                uint32_t v[16];
+                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+                uint32_t hi[8], lo[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    float x0 = __uint_as_float(v[2 * j]), x1 = __uint_as_float(v[2 * j + 1]);
+                    __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+                    hi[j] = pack_bf162(__bfloat162float(h0), __bfloat162float(h1));
+                    lo[j] = pack_bf162(x0 - __bfloat162float(h0), x1 - __bfloat162float(h1));
+                }
+                uint4* dh = reinterpret_cast<uint4*>(a.Xhi + base + c0);
+                uint4* dl = reinterpret_cast<uint4*>(a.Xlo + base + c0);
+                dh[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                dh[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
+                dl[0] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                dl[1] = make_uint4(lo[4], lo[5], lo[6], lo[7]);
+            }
+        } else {
+            float* dst = a.part + (((size_t)split * a.ntiles_out + tile) * MM + r) * MM;
+            for (int c0 = 0; c0 < MM; c0 += 16) {
+                uint32_t v[16];
+                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+                float4* d4 = reinterpret_cast<float4*>(dst + c0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    d4[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                                        __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+            }
+        }
+    }
+    if (*abort_flag && threadIdx.x == 0) {
+        // let copies already issued land before the block's shared memory goes away
+        uint64_t t0 = tc::global_timer();
+        while (tc::global_timer() - t0 < 10000000ull) {
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+}
+
+// ---------------------------------------------------------------- helper kernels
+// Dense BF16 hi/lo slices of B (both triangles) from the FP64 tiles: rows (Q, m), columns n.
+__global__ void split_B_kernel(const double* __restrict__ B, int naux, int nbf, int nT, int ntiles,
+                               const int* __restrict__ map, int nbf_p, __nv_bfloat16* __restrict__ Bh,
+                               __nv_bfloat16* __restrict__ Bl) {
+    size_t row = blockIdx.x;  // Q * nbf_p + m
+    int Q = (int)(row / nbf_p), m = (int)(row % nbf_p);
+    for (int n = threadIdx.x; n < nbf_p; n += blockDim.x) {
+        double v = 0.0;
+        if (m < nbf && n < nbf) {
+            int I = m / TILE, J = n / TILE;
+            int hi = I >= J ? I : J, lo = I >= J ? J : I;
+            int t = map[hi * nT + lo];
+            if (t >= 0) {
+                size_t base = ((size_t)Q * ntiles + t) * TILE_ELEMS;
+                v = (I >= J) ? B[base + (m % TILE) * TILE + (n % TILE)] : B[base + (n % TILE) * TILE + (m % TILE)];
+            }
+        }
+        __nv_bfloat16 h = __double2bfloat16(v);
+        Bh[row * nbf_p + n] = h;
+        Bl[row * nbf_p + n] = __double2bfloat16(v - (double)__bfloat162float(h));
+    }
+}
+
+// U^T slices: row j < npos_pad holds column j of the positive group, row npos_pad + j holds
+// column npos + j (negative group); padding rows/columns are zero.
+__global__ void split_Ut_kernel(const double* __restrict__ U, int ldu, int nbf, int npos, int nneg, int npos_pad,
+                                int nu_pad, int nbf_p, __nv_bfloat16* __restrict__ Uh, __nv_bfloat16* __restrict__ Ul) {
+    size_t n = (size_t)nu_pad * nbf_p;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(e / nbf_p), k = (int)(e % nbf_p);
+        int col = -1;
+        if (j < npos_pad) {
+            if (j < npos) col = j;
+        } else if (j - npos_pad < nneg) {
+            col = npos + (j - npos_pad);
+        }
+        double v = (col >= 0 && k < nbf) ? U[(size_t)k * ldu + col] : 0.0;
+        __nv_bfloat16 h = __double2bfloat16(v);
+        Uh[e] = h;
+        Ul[e] = __double2bfloat16(v - (double)__bfloat162float(h));
+    }
+}
+
+// K[m][n] (and its mirror) = sum over splits (fixed order, FP64) of the partial tiles.
+__global__ void reduce_mixed_kernel(const float* __restrict__ part, int nsplit, int ntiles_out, int nbf,
+                                    double* __restrict__ K, int ldk, double* __restrict__ Kacc, int accumulate) {
+    int t = blockIdx.x;
+    int I, J;
+    tile_of(t, I, J);
+    for (int e = threadIdx.x; e < MM * MM; e += blockDim.x) {
+        int r = e / MM, c = e % MM;
+        int m = I * MM + r, n = J * MM + c;
+        if (m >= nbf || n >= nbf) continue;
+        if (I == J && m < n) continue;  // the diagonal tile's upper half comes from its lower
+        double s = 0.0;
+        for (int k = 0; k < nsplit; ++k) s += (double)part[(((size_t)k * ntiles_out + t) * MM + r) * MM + c];
+        if (I == J && m > n) {
+            // symmetrise the diagonal tile
+            double s2 = 0.0;
+            for (int k = 0; k < nsplit; ++k) s2 += (double)part[(((size_t)k * ntiles_out + t) * MM + c) * MM + r];
+            s = 0.5 * (s + s2);
+        }
+        if (accumulate) {
+            s += Kacc[(size_t)m * nbf + n];
+        }
+        if (Kacc) {
+            Kacc[(size_t)m * nbf + n] = s;
+            Kacc[(size_t)n * nbf + m] = s;
+        }
+        K[(size_t)m * ldk + n] = s;
+        K[(size_t)n * ldk + m] = s;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2D bf16 tensor [rows][cols] (cols contiguous), box {32, box_rows}, 64-byte swizzle.
+bool make_map(CUtensorMap* m, const void* base, unsigned long long cols, unsigned long long rows, int box_rows) {
+    auto enc = get_encode();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {cols, rows};
+    cuuint64_t strides[1] = {cols * 2};
+    cuuint32_t box[2] = {(cuuint32_t)MK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+int pow2_cols(int n) {
+    int c = 32;
+    while (c < n) c <<= 1;
+    return c;
+}
+
+}  // namespace
+
 struct MixedState {
-    int dummy = 0;
+    int nbf_p = 0;
+    __nv_bfloat16 *Bh = nullptr, *Bl = nullptr;  // naux*nbf_p x nbf_p
+    bool B_ready = false;
+    __nv_bfloat16 *Uh = nullptr, *Ul = nullptr;
+    size_t U_cap = 0;
+    __nv_bfloat16 *Xh = nullptr, *Xl = nullptr;
+    size_t X_cap = 0;
+    float* part = nullptr;
+    size_t part_cap = 0;
+    double* Kacc = nullptr;  // running K of incremental builds (nbf x nbf)
+    size_t Kacc_cap = 0;
+    bool have_prev = false;
+    int* err = nullptr;
+    bool attrs_set = false;
 };
 
 MixedState* mixed_create() { return new MixedState(); }
-void mixed_destroy(MixedState* m) { delete m; }
-void mixed_invalidate(MixedState*) {}
-size_t mixed_query_memory(int, int, int) { return 0; }
-int mixed_build_K(MixedState*, const double*, const TileLayout&, int, int, int, const double*, int, int, int, double*,
-                  cudaEvent_t, cudaStream_t, std::string& err) {
-    err = "mixed-precision K is not available in this build";
-    return GDFJK_ERR_ARG;
+
+static void free_all(MixedState* m) {
+    void* ps[] = {m->Bh, m->Bl, m->Uh, m->Ul, m->Xh, m->Xl, m->part, m->Kacc, m->err};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    m->Bh = m->Bl = m->Uh = m->Ul = m->Xh = m->Xl = nullptr;
+    m->part = nullptr;
+    m->Kacc = nullptr;
+    m->err = nullptr;
+    m->U_cap = m->X_cap = m->part_cap = m->Kacc_cap = 0;
+    m->B_ready = false;
+    m->have_prev = false;
+}
+
+void mixed_destroy(MixedState* m) {
+    if (!m) return;
+    free_all(m);
+    delete m;
+}
+
+void mixed_invalidate(MixedState* m) {
+    if (!m) return;
+    if (m->Bh) cudaFree(m->Bh);
+    if (m->Bl) cudaFree(m->Bl);
+    m->Bh = m->Bl = nullptr;
+    m->B_ready = false;
+    m->have_prev = false;
+}
+
+size_t mixed_query_memory(int nbf, int naux, int max_nocc) {
+    size_t nbf_p = (size_t)round_up(nbf, MM);
+    size_t nu = (size_t)round_up(std::max(1, 2 * max_nocc), 64) + 64;
+    size_t b = 2 * 2 * (size_t)naux * nbf_p * nbf_p;  // B slices
+    b += 2 * 2 * nbf_p * naux * nu;                   // X slices
+    b += 2 * 2 * nu * nbf_p + nbf_p * nbf_p * 8;
+    return b;
+}
+
+static int dalloc_bytes(void** p, size_t bytes, std::string& err) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = "mixed: device allocation of " + std::to_string(bytes / 1e9) + " GB refused";
+        return GDFJK_ERR_OOM;
+    }
+    return GDFJK_OK;
+}
+
+// K_inc (written into K, nbf x nbf) = sum_Q B_Q (U+ U+^T - U- U-^T) B_Q; if `accumulate`,
+// the running K is added and updated.
+int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf, int naux, const double* U, int ldu,
+                   int npos, int nneg, int accumulate, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
+                   std::string& err) {
+    int rc;
+    const int nbf_p = round_up(nbf, MM);
+    if (!m->err) {
+        if ((rc = dalloc_bytes((void**)&m->err, sizeof(int), err))) return rc;
+        cudaMemsetAsync(m->err, 0, sizeof(int), s);
+    }
+    if (!m->B_ready || m->nbf_p != nbf_p) {
+        size_t bytes = (size_t)naux * nbf_p * nbf_p * 2;
+        if ((rc = dalloc_bytes((void**)&m->Bh, bytes, err)) || (rc = dalloc_bytes((void**)&m->Bl, bytes, err))) return rc;
+        split_B_kernel<<<(unsigned)((size_t)naux * nbf_p), 256, 0, s>>>(B, naux, nbf, L.nT, L.ntiles, L.map, nbf_p, m->Bh,
+                                                                       m->Bl);
+        m->nbf_p = nbf_p;
+        m->B_ready = true;
+    }
+    const int npos_pad = round_up(npos, 64);
+    const int nneg_pad = round_up(nneg, 64);
+    const int nu_pad = npos_pad + nneg_pad;
+    if (nu_pad == 0) {
+        cudaMemsetAsync(K, 0, sizeof(double) * (size_t)nbf * nbf, s);
+        if (ev_transform_done) cudaEventRecord(ev_transform_done, s);
+        return GDFJK_OK;
+    }
+    size_t ue = (size_t)nu_pad * nbf_p;
+    if (ue > m->U_cap) {
+        if ((rc = dalloc_bytes((void**)&m->Uh, ue * 2, err)) || (rc = dalloc_bytes((void**)&m->Ul, ue * 2, err))) return rc;
+        m->U_cap = ue;
+    }
+    const unsigned long long kdim = (unsigned long long)naux * nu_pad;
+    size_t xe = (size_t)nbf_p * kdim;
+    if (xe > m->X_cap) {
+        if ((rc = dalloc_bytes((void**)&m->Xh, xe * 2, err)) || (rc = dalloc_bytes((void**)&m->Xl, xe * 2, err))) return rc;
+        m->X_cap = xe;
+    }
+    {
+        int blocks = (int)std::min<size_t>((ue + 255) / 256, 152 * 16);
+        split_Ut_kernel<<<blocks, 256, 0, s>>>(U, ldu, nbf, npos, nneg, npos_pad, nu_pad, nbf_p, m->Uh, m->Ul);
+    }
+    if (!m->attrs_set) {
+        cudaFuncSetAttribute(tc_gemm_kernel<MODE_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(tc_gemm_kernel<MODE_CONTRACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        m->attrs_set = true;
+    }
+    // ---- half-transform, in accumulator chunks of at most 448 columns
+    CUtensorMap mBh, mBl, mUh, mUl, mXh, mXl;
+    if (!make_map(&mBh, m->Bh, nbf_p, (unsigned long long)naux * nbf_p, MM) ||
+        !make_map(&mBl, m->Bl, nbf_p, (unsigned long long)naux * nbf_p, MM) ||
+        !make_map(&mUh, m->Uh, nbf_p, nu_pad, B_ROWS_PER_TMA) || !make_map(&mUl, m->Ul, nbf_p, nu_pad, B_ROWS_PER_TMA) ||
+        !make_map(&mXh, m->Xh, kdim, nbf_p, MM) || !make_map(&mXl, m->Xl, kdim, nbf_p, MM)) {
+        err = "mixed: cuTensorMapEncodeTiled failed";
+        return GDFJK_ERR_CUDA;
+    }
+    for (int n_off = 0; n_off < nu_pad; n_off += 448) {
+        TcArgs ta{};
+        ta.nbf_p = nbf_p;
+        ta.nu_pad = nu_pad;
+        ta.npos_pad = npos_pad;
+        ta.n_cols = std::min(448, nu_pad - n_off);
+        ta.n_off = n_off;
+        ta.kdim = kdim;
+        ta.Xhi = m->Xh;
+        ta.Xlo = m->Xl;
+        ta.err = m->err;
+        int stage_bytes = 2 * A_TILE_BYTES + 2 * ta.n_cols * MK * 2;
+        ta.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / stage_bytes);
+        ta.tmem_cols = pow2_cols(ta.n_cols);
+        unsigned grid = (unsigned)((size_t)naux * nbf_p / MM);
+        tc_gemm_kernel<MODE_TRANSFORM><<<grid, 128, SMEM_BUDGET, s>>>(mBh, mBl, mUh, mUl, ta);
+    }
+    if (ev_transform_done) cudaEventRecord(ev_transform_done, s);
+    // ---- contraction
+    const int ntr = nbf_p / MM;
+    const int ntiles_out = ntr * (ntr + 1) / 2;
+    const int nkb_total = (int)(kdim / MK);
+    int nsplit = std::max(1, (152 * 2 + ntiles_out - 1) / ntiles_out);
+    nsplit = std::min(nsplit, std::max(1, nkb_total / 16));
+    int kb_per_split = (nkb_total + nsplit - 1) / nsplit;
+    nsplit = (nkb_total + kb_per_split - 1) / kb_per_split;
+    size_t pe = (size_t)nsplit * ntiles_out * MM * MM;
+    if (pe > m->part_cap) {
+        if ((rc = dalloc_bytes((void**)&m->part, pe * 4, err))) return rc;
+        m->part_cap = pe;
+    }
+    TcArgs ca{};
+    ca.nbf_p = nbf_p;
+    ca.nu_pad = nu_pad;
+    ca.npos_pad = npos_pad;
+    ca.n_cols = MM;
+    ca.kdim = kdim;
+    ca.ntr = ntr;
+    ca.kb_per_split = kb_per_split;
+    ca.nkb_total = nkb_total;
+    ca.ntiles_out = ntiles_out;
+    ca.part = m->part;
+    ca.err = m->err;
+    ca.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / (4 * A_TILE_BYTES));
+    ca.tmem_cols = MM;
+    dim3 cgrid(ntiles_out, nsplit);
+    tc_gemm_kernel<MODE_CONTRACT><<<cgrid, 128, SMEM_BUDGET, s>>>(mXh, mXl, mXh, mXl, ca);
+    // ---- fixed-order FP64 reduction (+ running K for incremental builds)
+    size_t kn = (size_t)nbf * nbf;
+    if (kn > m->Kacc_cap) {
+        if ((rc = dalloc_bytes((void**)&m->Kacc, kn * 8, err))) return rc;
+        m->Kacc_cap = kn;
+        m->have_prev = false;
+    }
+    int acc = (accumulate && m->have_prev) ? 1 : 0;
+    reduce_mixed_kernel<<<ntiles_out, 256, 0, s>>>(m->part, nsplit, ntiles_out, nbf, K, nbf, m->Kacc, acc);
+    m->have_prev = true;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("mixed: launch failed: ") + cudaGetErrorString(e);
+        return GDFJK_ERR_CUDA;
+    }
+    return GDFJK_OK;
+}
+
+int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, int nbf, int nbf_pad, int naux,
+                  const double* Cpad, int nocc, int nocc_pad, int mode, double* K, cudaEvent_t ev_transform_done,
+                  cudaStream_t stream, std::string& err) {
+    (void)nbf_pad;
+    (void)mode;
+    // a full build: U = C_occ, all columns positive
+    return mixed_k_factor(m, B, L, nbf, naux, Cpad, nocc_pad, nocc, 0, 0, K, ev_transform_done, stream, err);
+}
+
+int mixed_error_flag(MixedState* m, cudaStream_t s) {
+    if (!m || !m->err) return 0;
+    int f = 0;
+    cudaMemcpyAsync(&f, m->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (f) cudaMemsetAsync(m->err, 0, sizeof(int), s);
+    return f;
 }
 
 }  // namespace gdfjk

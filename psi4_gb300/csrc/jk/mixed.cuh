@@ -21,4 +21,11 @@ int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, int nbf, 
                   const double* Cpad, int nocc, int nocc_pad, int mode, double* K, cudaEvent_t ev_transform_done,
                   cudaStream_t stream, std::string& err);
 
+// K (nbf x nbf, device) = [K_prev +] sum_Q B_Q (U+ U+^T - U- U-^T) B_Q, U device (nbf x nu, ldu).
+int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf, int naux, const double* U, int ldu,
+                   int npos, int nneg, int accumulate, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
+                   std::string& err);
+// error bits raised by the tensor-core kernels since the last call (0 = none); clears them
+int mixed_error_flag(MixedState* m, cudaStream_t s);
+
 }  // namespace gdfjk

@@ -90,6 +90,19 @@ class DFJKEngine:
                                          nocc, max(nocc, 1), mode, _p(D), _p(J), _p(K)))
         return J, K, D
 
+    def compute_incremental(self, C, U, npos, mode=abi.DO_J | abi.DO_K, reset=False):
+        """Precision form: J (FP64) from C; K = K_prev + sum_Q B_Q (U+U+^T - U-U-^T) B_Q in
+        split BF16 with FP32 accumulation (K_prev = 0 when reset)."""
+        C = np.ascontiguousarray(C, dtype=np.float64)
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        nocc, nu = C.shape[1], U.shape[1]
+        J = np.empty((self.nbf, self.nbf))
+        K = np.empty((self.nbf, self.nbf))
+        m = mode | (abi.RESET if reset else 0)
+        self._check(self.L.gdfjk_compute_incremental(self.h, _p(C) if nocc else None, nocc, max(nocc, 1),
+                                                     _p(U) if nu else None, nu, int(npos), max(nu, 1), m, _p(J), _p(K)))
+        return J, K
+
     def compute_device(self, Cl_ptr, Cr_ptr, nocc, ldc, mode, D_ptr, J_ptr, K_ptr):
         vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
         self._check(self.L.gdfjk_compute_device(self.h, vp(Cl_ptr), vp(Cr_ptr), int(nocc), int(ldc), int(mode), vp(D_ptr),
@@ -142,6 +155,25 @@ class DFJKEngine:
             pass
 
 
+def density_difference_factor(C_new, C_old, tol=1e-13):
+    """Signed low-rank factor of dD = C_new C_new^T - C_old C_old^T.
+
+    QR of [C_new, C_old] = Q R gives dD = Q (R S R^T) Q^T with S = diag(+1.., -1..); the small
+    symmetric R S R^T = W diag(lam) W^T then gives dD = U+ U+^T - U- U-^T with
+    U = Q W |lam|^1/2, positive eigenvalues first.  Eigenvalues below `tol` are dropped.
+    Returns (U, npos)."""
+    A = np.hstack([C_new, C_old])
+    Q, R = np.linalg.qr(A)
+    sgn = np.concatenate([np.ones(C_new.shape[1]), -np.ones(C_old.shape[1])])
+    lam, W = np.linalg.eigh((R * sgn) @ R.T)
+    keep = np.abs(lam) > tol
+    lam, W = lam[keep], W[:, keep]
+    order = np.argsort(-lam)
+    lam, W = lam[order], W[:, order]
+    U = (Q @ W) * np.sqrt(np.abs(lam))
+    return np.ascontiguousarray(U), int((lam > 0).sum())
+
+
 class GpuDFJK:
     """A drop-in for psi4's MemDFJK in an RHF loop, served by the GB300 engine."""
 
@@ -161,6 +193,8 @@ class GpuDFJK:
         self._Cl, self._Cr = [], []
         self._J, self._K, self._D = [], [], []
         self.last_timings = {}
+        self._C_prev = None
+        self.last_rank = 0
 
     # psi4: core.JK.build(orbital_basis, aux, jk_type=...)
     @staticmethod
@@ -199,6 +233,10 @@ class GpuDFJK:
 
     def set_incremental(self, v: bool):
         self.incremental = bool(v)
+
+    def reset_incremental(self):
+        """Forget the previous density: the next mixed build is a full build."""
+        self._C_prev = None
 
     def C1(self):
         return True
@@ -255,6 +293,24 @@ class GpuDFJK:
             if self.incremental:
                 mode |= abi.INCREMENTAL
         self._J, self._K, self._D = [], [], []
+        if self.precision == "mixed" and lr_symmetric and self.do_K and len(self._Cl) == 1:
+            # the precision form: K from the split-BF16 tensor-core path, incremental over dD
+            C = self._Cl[0]
+            jmode = (abi.DO_J if self.do_J else 0) | abi.DO_K
+            if self.incremental and self._C_prev is not None and self._C_prev.shape == C.shape:
+                U, npos = density_difference_factor(C, self._C_prev)
+                J, K = self.engine.compute_incremental(C, U, npos, mode=jmode, reset=False)
+                self.last_rank = U.shape[1]
+            else:
+                J, K = self.engine.compute_incremental(C, C, C.shape[1], mode=jmode, reset=True)
+                self.last_rank = C.shape[1]
+            self._C_prev = C.copy()
+            self._J.append(J if self.do_J else None)
+            self._K.append(K)
+            self._D.append(C @ C.T)
+            self.last_timings = self.engine.timings()
+            return
+        self._C_prev = None
         for i, Cl in enumerate(self._Cl):
             Cr = None if lr_symmetric else self._Cr[i]
             if Cr is not None and Cr.shape[1] != Cl.shape[1]:

@@ -87,9 +87,43 @@ class DIIS:
         return sum(ci * Fi for ci, Fi in zip(c, self.F))
 
 
+class PrecisionSchedule:
+    """The precision form's build schedule for a GpuDFJK: split-BF16 incremental K builds
+    (over dD) while far from convergence, FP64 full rebuilds once the mixed iterations reach
+    |dE| < switch_e and RMS gradient < switch_d (or after max_mixed of them).  Convergence is
+    only accepted on an FP64 build that follows another FP64 build, so the final two Fock
+    builds are full FP64 rebuilds and the converged energy is an FP64 energy."""
+
+    def __init__(self, switch_e=1e-6, switch_d=1e-5, max_mixed=60, report_fp64=None):
+        self.switch_e, self.switch_d, self.max_mixed = switch_e, switch_d, max_mixed
+        self.report_fp64 = report_fp64  # optional JK (FP64) to measure each mixed energy's error
+        self.mode = "mixed"
+        self.n_mixed = 0
+        self.n_fp64 = 0
+        self.fp64_streak = 0
+
+    def before(self, jk):
+        jk.set_precision(self.mode)
+        jk.set_incremental(self.mode == "mixed")
+
+    def after(self, dE, dnorm):
+        if self.mode == "mixed":
+            self.n_mixed += 1
+            self.fp64_streak = 0
+            if (abs(dE) < self.switch_e and dnorm < self.switch_d) or self.n_mixed >= self.max_mixed:
+                self.mode = "fp64"
+        else:
+            self.n_fp64 += 1
+            self.fp64_streak += 1
+
+    def may_converge(self):
+        return self.fp64_streak >= 2
+
+
 def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=None, diis_start=1,
-        fail_on_maxiter=True, callback=None, verbose=False) -> SCFResult:
-    """Run RHF with a JK object exposing C_clear/C_left_add/compute/J/K."""
+        fail_on_maxiter=True, callback=None, verbose=False, schedule: PrecisionSchedule | None = None) -> SCFResult:
+    """Run RHF with a JK object exposing C_clear/C_left_add/compute/J/K.  With a
+    PrecisionSchedule the JK switches between the mixed and FP64 forms per iteration."""
     X = orthogonalizer(S)
     t0 = time.perf_counter()
     if guess_C is None:
@@ -112,6 +146,10 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
         D = Cocc @ Cocc.T
         jk.C_clear()
         jk.C_left_add(Cocc)
+        mode = None
+        if schedule is not None:
+            schedule.before(jk)
+            mode = schedule.mode
         tj = time.perf_counter()
         jk.compute()
         t_jk += time.perf_counter() - tj
@@ -123,12 +161,25 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
         grad = X.T @ (F @ D @ S - S @ D @ F) @ X
         dnorm = float(np.sqrt(np.mean(grad * grad)))
         dE = E - E_old
-        log.append({"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm})
+        entry = {"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm}
+        if mode is not None:
+            entry["precision"] = mode
+            if mode == "mixed" and schedule.report_fp64 is not None:
+                ref = schedule.report_fp64
+                ref.C_clear()
+                ref.C_left_add(Cocc)
+                ref.compute()
+                Jr, Kr = np.asarray(ref.J()[0]), np.asarray(ref.K()[0])
+                Er = e_nuc + 2.0 * np.vdot(D, H) + 2.0 * np.vdot(D, Jr) - np.vdot(D, Kr)
+                entry["energy_error_vs_fp64"] = float(E - Er)
+        log.append(entry)
         if verbose:
-            print(f"  @RHF iter {it:3d}: {E:20.14f} {dE: .3e} {dnorm: .3e}")
+            print(f"  @RHF iter {it:3d}: {E:20.14f} {dE: .3e} {dnorm: .3e} {mode or ''}")
         if callback is not None:
             callback(it, E, dE, dnorm, D)
-        if abs(dE) < e_conv and dnorm < d_conv:
+        if schedule is not None:
+            schedule.after(dE, dnorm)
+        if abs(dE) < e_conv and dnorm < d_conv and (schedule is None or schedule.may_converge()):
             converged = True
             break
         E_old = E
