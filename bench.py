@@ -50,6 +50,10 @@ def workload_sizes(cfg):
     from psi4_gb300.basis import BasisSet
     from psi4_gb300.molecule import linear_alkane, water_cluster
 
+    if cfg.startswith("synthetic:"):
+        # "synthetic:nbf,naux,nocc" — a seeded synthetic shape (profiling captures)
+        nbf, naux, nocc = (int(x) for x in cfg.split(":")[1].split(","))
+        return None, nbf, naux, nocc, f"synthetic nbf {nbf} naux {naux} nocc {nocc}"
     gen, basis, desc = CONFIGS[cfg]
     mol = water_cluster(*gen["lattice"], seed=0) if "lattice" in gen else linear_alkane(gen["alkane"], seed=0)
     pb = BasisSet.build(mol, basis)
@@ -264,6 +268,7 @@ def run_gpu(args):
                   "peak": hbm, "unit": "GB/s", "frac": bytes_j / jt / 1e9 / hbm,
                   "algorithmic_bytes_per_build": bytes_j, "note": "of measured"}
 
+    args._fp64_value = value / ws
     out = {"metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded B of the workload's shape, generated on device; real C-shaped orbitals)",
@@ -275,35 +280,123 @@ def run_gpu(args):
                         "k_contract": statistics.median(kc_ms)},
            "clocks": clk, "gpu_launches": 10 * args.steps}
 
-    # split-precision K at the same shape (device-resident), if built
+    # the precision form at the same shape (device-resident): split-BF16 tensor-core K
     if args.mixed:
         try:
-            mm = mode | abi.MIXED
-            for _ in range(2):
-                step_device(mm)
-            eng.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(args.steps):
-                step_device(mm)
-            e1.record(stream)
-            eng.synchronize()
-            tm = eng.timings()
-            tmix = e0.elapsed_time(e1) / 1e3 / args.steps
-            out["mixed"] = {"builds_per_s": 1.0 / tmix, "ms_per_build": 1e3 * tmix, "phase_ms": tm,
-                            "speedup_vs_fp64": ms_per_step / (1e3 * tmix)}
+            out["mixed"] = measure_mixed(eng, C, J, K, nbf, naux, nocc, stream, args, peaks)
         except Exception as ex:  # reported, not hidden
-            out["mixed"] = {"unavailable": str(ex)[:200]}
+            out["mixed"] = {"unavailable": str(ex)[:300]}
 
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(nbf, naux, nocc, budget_s=args.cpu_budget)
+    if rank == 0 and args.scf:
+        try:
+            out["scf"] = measure_scf(args.scf_config)
+        except Exception as ex:
+            out["scf"] = {"unavailable": str(ex)[:300]}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def measure_mixed(eng, C, J, K, nbf, naux, nocc, stream, args, peaks):
+    """Builds/s of the precision form at the bench shape: a full split-BF16 build from C and
+    an incremental build over a rank-2*nocc signed factor of dD (the size an SCF step has)."""
+    import torch
+
+    from psi4_gb300 import _jkabi as abi
+
+    dev = C.device
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(99)
+    mm = abi.DO_J | abi.DO_K | abi.MIXED
+
+    def full():
+        eng.compute_device(C.data_ptr(), None, nocc, nocc, mm, None, J.data_ptr(), K.data_ptr())
+
+    def timed(fn, n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        eng.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / n
+
+    for _ in range(2):
+        full()
+    eng.synchronize()
+    t_full = timed(full, args.steps)
+    tm_full = eng.timings()
+    # incremental: host buffers through gdfjk_compute_incremental, rank 2*nocc factor
+    Ch = C.cpu().numpy()
+    U = (torch.randn((nbf, 2 * nocc), dtype=torch.float64, device=dev, generator=gen) * 1e-3).cpu().numpy()
+    eng.compute_incremental(Ch, U, nocc, reset=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.compute_incremental(Ch, U, nocc, reset=False)
+    t_inc = (time.perf_counter() - t0) / args.steps
+    tm_inc = eng.timings()
+    nbf_p = -(-nbf // 128) * 128
+    nu_full = -(-nocc // 64) * 64
+    # issued BF16 tensor work of the half-transform (3 products) vs the measured bf16 peak
+    issued = 3 * 2.0 * naux * nbf_p * nbf_p * nu_full
+    kt = tm_full["k_transform_ms"] / 1e3
+    peak = float(peaks.get("bf16_tflops", 1885.4))
+    return {
+        "full_builds_per_s": 1.0 / t_full, "full_ms_per_build": 1e3 * t_full, "full_phase_ms": tm_full,
+        "incremental_builds_per_s": 1.0 / t_inc, "incremental_ms_per_build_e2e": 1e3 * t_inc, "incremental_rank": 2 * nocc,
+        "incremental_phase_ms": tm_inc, "speedup_full_vs_fp64": (1.0 / t_full) / (args._fp64_value or 1e-30),
+        "roofline_transform": {"bound": "tensor", "kernel": "tc_gemm_kernel<transform>", "achieved": issued / kt / 1e12,
+                               "peak": peak, "unit": "TFLOP/s", "frac": issued / kt / 1e12 / peak,
+                               "note": "issued BF16 flops (3 split products, padded sizes) of measured burst bf16"},
+        "scheme": "BF16x3: x = hi + lo (bf16), products hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM, FP64 split-K reduction",
+    }
+
+
+def measure_scf(cfg):
+    """SCF time-to-converge on real integrals: FP64-GPU form vs the precision form."""
+    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.dfhelper import build_df_tensor
+    from psi4_gb300.ints import Integrals
+    from psi4_gb300.jk import GpuDFJK
+    from psi4_gb300.molecule import water_cluster
+    from psi4_gb300.scf import PrecisionSchedule, core_hamiltonian, rhf
+
+    gen, basis, desc = CONFIGS[cfg]
+    mol = water_cluster(*gen["lattice"], seed=0)
+    pb = BasisSet.build(mol, basis)
+    ab = BasisSet.fitting_for(mol, pb)
+    t0 = time.perf_counter()
+    ints = Integrals(mol, pb, ab)
+    df = build_df_tensor(mol, pb, ab, ints=ints)
+    H, S = core_hamiltonian(ints), ints.overlap()
+    t_init = time.perf_counter() - t0
+    nocc = mol.nelectron // 2
+    jk = GpuDFJK.from_tensor(df)
+    jk.initialize()
+    # warm the CUDA context and both paths once
+    jk.C_clear(); jk.C_left_add(np.eye(df.nbf)[:, :nocc]); jk.compute()
+    jk.set_precision("mixed"); jk.compute(); jk.set_precision("fp64")
+    t0 = time.perf_counter()
+    r64 = rhf(jk, H, S, nocc, mol.nuclear_repulsion_energy())
+    t64 = time.perf_counter() - t0
+    jk.reset_incremental()
+    sched = PrecisionSchedule()
+    t0 = time.perf_counter()
+    rmx = rhf(jk, H, S, nocc, mol.nuclear_repulsion_energy(), schedule=sched)
+    tmx = time.perf_counter() - t0
+    return {"workload": desc + " (real integrals, e_conv 1e-10, d_conv 1e-8, core guess)", "nbf": df.nbf,
+            "naux": df.naux, "nocc": nocc, "init_s": t_init,
+            "fp64": {"energy": r64.energy, "iterations": r64.iterations, "seconds": t64, "jk_seconds": r64.timings["jk_s"]},
+            "precision_form": {"energy": rmx.energy, "mixed_builds": sched.n_mixed, "fp64_builds": sched.n_fp64,
+                               "seconds": tmx, "jk_seconds": rmx.timings["jk_s"]},
+            "abs_energy_difference": abs(rmx.energy - r64.energy),
+            "time_to_converge_speedup": t64 / tmx}
 
 
 def run_reference(args):
@@ -341,11 +434,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c2", help="c1..c5 or synthetic:nbf,naux,nocc")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--mixed", type=int, default=1)
+    ap.add_argument("--scf", type=int, default=1)
+    ap.add_argument("--scf-config", default="c4", choices=["c1", "c4"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -87,7 +87,9 @@ int gdfjk_compute_device(gdfjk_t h, const double* C_left, const double* C_right,
  * as a split-BF16 tensor-core product with FP32 accumulation, where U (nbf x nu, leading
  * dimension ldu) holds npos positive columns then nu - npos negative ones, a signed factor
  * of dD = D - D_prev.  K_prev is the K this handle returned last (kept on the device in
- * FP64); GDFJK_RESET in mode takes K_prev = 0, i.e. a full build from the factor. */
+ * FP64); GDFJK_RESET in mode takes K_prev = 0, i.e. a full build from the factor.
+ * Without GDFJK_MIXED in mode, K is instead a full FP64 build from C (U is ignored) and
+ * becomes the base K_prev of the following increments (an FP64 re-anchor). */
 int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
                               int mode, double* J, double* K);
 

@@ -530,7 +530,16 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
                            nullptr);
         if (rc) return rc;
     }
-    if (mode & GDFJK_DO_K) {
+    if ((mode & GDFJK_DO_K) && !(mode & GDFJK_MIXED)) {
+        // FP64 anchor: a full FP64 K from C that becomes the base of later increments
+        rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_K, nullptr, nullptr,
+                           h->dK);
+        if (rc) return rc;
+        rc = mixed_set_base(h->mixed, h->dK, h->nbf, s, h->err);
+        if (rc) return rc;
+        launch_finite_check(h->dK, n2, h->d_err, s);
+        CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
+    } else if (mode & GDFJK_DO_K) {
         CK(cudaEventRecord(h->ev[2], s));
         rc = mixed_k_factor(h->mixed, h->B, layout_of(h), h->nbf, h->naux, h->dCrin, std::max(ldu, 1), npos, nu - npos,
                             (mode & GDFJK_RESET) ? 0 : 1, h->dK, h->ev[3], s, h->err);

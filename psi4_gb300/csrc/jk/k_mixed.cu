@@ -545,6 +545,21 @@ int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, int nbf, 
     return mixed_k_factor(m, B, L, nbf, naux, Cpad, nocc_pad, nocc, 0, 0, K, ev_transform_done, stream, err);
 }
 
+int mixed_set_base(MixedState* m, const double* K, int nbf, cudaStream_t s, std::string& err) {
+    size_t kn = (size_t)nbf * nbf;
+    if (kn > m->Kacc_cap) {
+        int rc = dalloc_bytes((void**)&m->Kacc, kn * 8, err);
+        if (rc) return rc;
+        m->Kacc_cap = kn;
+    }
+    if (cudaMemcpyAsync(m->Kacc, K, kn * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+        err = "mixed: copying the FP64 base failed";
+        return GDFJK_ERR_CUDA;
+    }
+    m->have_prev = true;
+    return GDFJK_OK;
+}
+
 int mixed_error_flag(MixedState* m, cudaStream_t s) {
     if (!m || !m->err) return 0;
     int f = 0;

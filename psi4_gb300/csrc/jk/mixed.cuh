@@ -25,6 +25,8 @@ int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, int nbf, 
 int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf, int naux, const double* U, int ldu,
                    int npos, int nneg, int accumulate, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
                    std::string& err);
+// Make K (device, nbf x nbf, FP64) the base of the next incremental build.
+int mixed_set_base(MixedState* m, const double* K, int nbf, cudaStream_t s, std::string& err);
 // error bits raised by the tensor-core kernels since the last call (0 = none); clears them
 int mixed_error_flag(MixedState* m, cudaStream_t s);
 

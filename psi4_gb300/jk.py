@@ -90,9 +90,10 @@ class DFJKEngine:
                                          nocc, max(nocc, 1), mode, _p(D), _p(J), _p(K)))
         return J, K, D
 
-    def compute_incremental(self, C, U, npos, mode=abi.DO_J | abi.DO_K, reset=False):
+    def compute_incremental(self, C, U, npos, mode=abi.DO_J | abi.DO_K | abi.MIXED, reset=False):
         """Precision form: J (FP64) from C; K = K_prev + sum_Q B_Q (U+U+^T - U-U-^T) B_Q in
-        split BF16 with FP32 accumulation (K_prev = 0 when reset)."""
+        split BF16 with FP32 accumulation (K_prev = 0 when reset).  Without MIXED in mode,
+        K is a full FP64 build from C that becomes the base of later increments."""
         C = np.ascontiguousarray(C, dtype=np.float64)
         U = np.ascontiguousarray(U, dtype=np.float64)
         nocc, nu = C.shape[1], U.shape[1]
@@ -293,10 +294,20 @@ class GpuDFJK:
             if self.incremental:
                 mode |= abi.INCREMENTAL
         self._J, self._K, self._D = [], [], []
+        if self.precision == "fp64" and self.incremental and lr_symmetric and self.do_K and len(self._Cl) == 1:
+            # FP64 re-anchor of the precision form: full FP64 K, kept as the incremental base
+            C = self._Cl[0]
+            J, K = self.engine.compute_incremental(C, C, C.shape[1], mode=(abi.DO_J if self.do_J else 0) | abi.DO_K)
+            self._C_prev = C.copy()
+            self._J.append(J if self.do_J else None)
+            self._K.append(K)
+            self._D.append(C @ C.T)
+            self.last_timings = self.engine.timings()
+            return
         if self.precision == "mixed" and lr_symmetric and self.do_K and len(self._Cl) == 1:
             # the precision form: K from the split-BF16 tensor-core path, incremental over dD
             C = self._Cl[0]
-            jmode = (abi.DO_J if self.do_J else 0) | abi.DO_K
+            jmode = (abi.DO_J if self.do_J else 0) | abi.DO_K | abi.MIXED
             if self.incremental and self._C_prev is not None and self._C_prev.shape == C.shape:
                 U, npos = density_difference_factor(C, self._C_prev)
                 J, K = self.engine.compute_incremental(C, U, npos, mode=jmode, reset=False)

@@ -88,30 +88,47 @@ class DIIS:
 
 
 class PrecisionSchedule:
-    """The precision form's build schedule for a GpuDFJK: split-BF16 incremental K builds
-    (over dD) while far from convergence, FP64 full rebuilds once the mixed iterations reach
-    |dE| < switch_e and RMS gradient < switch_d (or after max_mixed of them).  Convergence is
-    only accepted on an FP64 build that follows another FP64 build, so the final two Fock
-    builds are full FP64 rebuilds and the converged energy is an FP64 energy."""
+    """The precision form's build schedule for a GpuDFJK.
 
-    def __init__(self, switch_e=1e-6, switch_d=1e-5, max_mixed=60, report_fp64=None):
-        self.switch_e, self.switch_d, self.max_mixed = switch_e, switch_d, max_mixed
+    1. split-BF16 incremental K builds (over dD) from the guess;
+    2. once the RMS orbital gradient drops below anchor_d: one FP64 full build that becomes
+       the base of the following increments (their errors then scale with the now small dD);
+    3. split-BF16 increments again until |dE| < switch_e and RMS gradient < switch_d;
+    4. FP64 full rebuilds to convergence.  Convergence is only accepted on an FP64 build that
+       follows another FP64 build, so the final two Fock builds are full FP64 rebuilds and
+       the converged energy is an FP64 energy."""
+
+    def __init__(self, anchor_d=1e-3, switch_e=1e-8, switch_d=1e-6, max_mixed=60, report_fp64=None):
+        self.anchor_d, self.switch_e, self.switch_d, self.max_mixed = anchor_d, switch_e, switch_d, max_mixed
         self.report_fp64 = report_fp64  # optional JK (FP64) to measure each mixed energy's error
         self.mode = "mixed"
+        self.anchored = anchor_d is None
         self.n_mixed = 0
         self.n_fp64 = 0
+        self.n_anchor = 0
         self.fp64_streak = 0
 
     def before(self, jk):
-        jk.set_precision(self.mode)
-        jk.set_incremental(self.mode == "mixed")
+        if self.mode == "anchor":
+            jk.set_precision("fp64")
+            jk.set_incremental(True)
+        else:
+            jk.set_precision(self.mode)
+            jk.set_incremental(self.mode == "mixed")
 
     def after(self, dE, dnorm):
         if self.mode == "mixed":
             self.n_mixed += 1
             self.fp64_streak = 0
-            if (abs(dE) < self.switch_e and dnorm < self.switch_d) or self.n_mixed >= self.max_mixed:
+            if not self.anchored and dnorm < self.anchor_d:
+                self.mode = "anchor"
+            elif (abs(dE) < self.switch_e and dnorm < self.switch_d) or self.n_mixed >= self.max_mixed:
                 self.mode = "fp64"
+        elif self.mode == "anchor":
+            self.n_anchor += 1
+            self.n_fp64 += 1
+            self.anchored = True
+            self.mode = "mixed"
         else:
             self.n_fp64 += 1
             self.fp64_streak += 1
@@ -164,7 +181,7 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
         entry = {"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm}
         if mode is not None:
             entry["precision"] = mode
-            if mode == "mixed" and schedule.report_fp64 is not None:
+            if mode in ("mixed", "anchor") and schedule.report_fp64 is not None:
                 ref = schedule.report_fp64
                 ref.C_clear()
                 ref.C_left_add(Cocc)

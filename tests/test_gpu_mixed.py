@@ -88,7 +88,7 @@ def test_precision_form_scf_h2o8(h2o8):
     sched = PrecisionSchedule(report_fp64=ref)
     rmx = rhf(jk, H, S, 40, mol.nuclear_repulsion_energy(), schedule=sched)
     errs = [e.get("energy_error_vs_fp64") for e in rmx.log if "energy_error_vs_fp64" in e]
-    print("fp64 iters", r64.iterations, "mixed", sched.n_mixed, "fp64 final", sched.n_fp64,
+    print("fp64 iters", r64.iterations, "mixed", sched.n_mixed, "fp64 (incl. anchor)", sched.n_fp64, "anchor", sched.n_anchor,
           "max |E_mixed - E_fp64| per iteration", max(abs(x) for x in errs))
     assert rmx.converged
     assert abs(rmx.energy - r64.energy) < 1e-6
