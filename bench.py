@@ -120,6 +120,36 @@ def dist_env():
     return ws, rank, local
 
 
+# ------------------------------------------------------------------ multi-rank helpers
+# Replicas only: every rank runs its own engine; the ranks meet only at barriers and for
+# the max of their timed regions (no collective on the data path).
+def dist_barrier(ws, dev):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    if dev is not None and dev.type == "cuda":
+        import torch
+
+        torch.cuda.synchronize(dev)
+
+
+def dist_max(x, ws, dev):
+    if ws == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_builds_per_s(ws, steps, t_max):
+    """Whole-job builds/s: all ranks' builds over the slowest rank's timed region."""
+    return ws * steps / t_max
+
+
 # ------------------------------------------------------------------ CPU leg (oracle)
 def cpu_restatement_time(nbf, naux_sample, nocc, threads, seed=1):
     """Time the oracle's restatement of DFHelper::compute_J_symm + compute_K on a Q-row
@@ -198,20 +228,10 @@ def run_gpu(args):
     eng.synchronize()
 
     def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-        torch.cuda.synchronize()
+        dist_barrier(ws, dev)
 
     def max_over_ranks(x):
-        if ws == 1:
-            return x
-        import torch.distributed as dist
-
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return dist_max(x, ws, dev)
 
     clocks = ClockSampler(local)
     barrier()
@@ -232,7 +252,7 @@ def run_gpu(args):
     clk = clocks.stop()
     t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
     ms_per_step = 1e3 * t_dev / args.steps
-    value = ws * args.steps / t_dev
+    value = aggregate_builds_per_s(ws, args.steps, t_dev)
 
     # e2e through the host-buffer C ABI call
     Ch = C.cpu().numpy()
@@ -243,7 +263,7 @@ def run_gpu(args):
         Jh, Kh, _ = eng.compute(Ch, mode=mode)
     barrier()
     t_e2e = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": ws * n_e2e / t_e2e, "unit": "builds/s", "h2d_bytes_per_step": int(Ch.nbytes),
+    e2e = {"value": aggregate_builds_per_s(ws, n_e2e, t_e2e), "unit": "builds/s", "h2d_bytes_per_step": int(Ch.nbytes),
            "d2h_bytes_per_step": int(Jh.nbytes + Kh.nbytes)}
 
     # roofline of the dominant kernel (FP64 half-transform): algorithmic flops per launch

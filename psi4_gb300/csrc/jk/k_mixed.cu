@@ -56,6 +56,8 @@ struct TcArgs {
     float* part;
     int stages;
     int tmem_cols;
+    int n_items;  // work items of this launch
+    int nbuf;     // TMEM accumulators (2 overlaps the epilogue with the next item)
     int* err;
 };
 
@@ -71,32 +73,26 @@ __device__ __forceinline__ uint32_t pack_bf162(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mAh,
-                                                         const __grid_constant__ CUtensorMap mAl,
-                                                         const __grid_constant__ CUtensorMap mBh,
-                                                         const __grid_constant__ CUtensorMap mBl, const TcArgs a) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const int N = a.n_cols;
-    const int b_bytes = N * MK * 2;
-    const int stage_bytes = 2 * A_TILE_BYTES + 2 * b_bytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * stage_bytes);
-    uint64_t* empty = full + a.stages;
-    uint64_t* accb = empty + a.stages;
-    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(accb + 1);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+// Persistent, warp-specialised GEMM: one CTA per SM walks the work items (round robin).
+// warp 0 lane 0: TMA producer over a ring of `stages` shared-memory stages;
+// warp 1 lane 0: tcgen05.mma issuer into one of `nbuf` TMEM accumulators;
+// warps 2-5:     epilogue (tcgen05.ld of the accumulator, then global stores), which
+//                overlaps the MMAs of the next item when nbuf == 2.
+constexpr int TC_THREADS = 192;
 
-    const int warp = threadIdx.x / 32;
-    int a_row, b_row, kb0, nkb, tile = 0, split = 0;
+template <int MODE>
+__device__ __forceinline__ void work_item(const TcArgs& a, int item, int& a_row, int& b_row, int& kb0, int& nkb,
+                                          int& tile, int& split) {
     if (MODE == MODE_TRANSFORM) {
-        a_row = blockIdx.x * MM;
+        a_row = item * MM;
         b_row = a.n_off;
         kb0 = 0;
         nkb = a.nbf_p / MK;
+        tile = item;
+        split = 0;
     } else {
-        tile = blockIdx.x;
-        split = blockIdx.y;
+        split = item / a.ntiles_out;  // split-major: concurrent CTAs share one k window in L2
+        tile = item % a.ntiles_out;
         int I, J;
         tile_of(tile, I, J);
         a_row = I * MM;
@@ -104,13 +100,36 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         kb0 = split * a.kb_per_split;
         nkb = min(a.kb_per_split, a.nkb_total - kb0);
     }
+}
 
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mAh,
+                                                                const __grid_constant__ CUtensorMap mAl,
+                                                                const __grid_constant__ CUtensorMap mBh,
+                                                                const __grid_constant__ CUtensorMap mBl, const TcArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int N = a.n_cols;
+    const int b_bytes = N * MK * 2;
+    const int stage_bytes = 2 * A_TILE_BYTES + 2 * b_bytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * stage_bytes);
+    uint64_t* empty = full + a.stages;
+    uint64_t* tfull = empty + a.stages;  // [2]
+    uint64_t* tempty = tfull + 2;        // [2]
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+
+    const int warp = threadIdx.x / 32;
+    const int nbuf = a.nbuf;
     if (threadIdx.x == 0) {
         for (int s = 0; s < a.stages; ++s) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        tc::mbar_init(accb, 1);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 4);
+        }
         *abort_flag = 0;
         tc::fence_barrier_init();
         tc::prefetch_tmap(&mAh);
@@ -126,102 +145,132 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
 
     if (threadIdx.x == 0) {
         // ---- TMA producer
-        for (int kb = 0; kb < nkb; ++kb) {
-            int s = kb % a.stages;
-            uint32_t ph = (uint32_t)((kb / a.stages) & 1);
-            if (kb >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) break;
-            uint8_t* st = smem + (size_t)s * stage_bytes;
-            tc::mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
-            int kx = (kb0 + kb) * MK;
-            tc::tma_load_2d(st, &mAh, &full[s], kx, a_row);
-            tc::tma_load_2d(st + A_TILE_BYTES, &mAl, &full[s], kx, a_row);
-            if (MODE == MODE_TRANSFORM) {
-                for (int r = 0; r < N; r += B_ROWS_PER_TMA) {
-                    tc::tma_load_2d(st + 2 * A_TILE_BYTES + r * MK * 2, &mBh, &full[s], kx, b_row + r);
-                    tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, &mBl, &full[s], kx, b_row + r);
+        long kg = 0;
+        for (int item = blockIdx.x; item < a.n_items && !*abort_flag; item += gridDim.x) {
+            int a_row, b_row, kb0, nkb, tile, split;
+            work_item<MODE>(a, item, a_row, b_row, kb0, nkb, tile, split);
+            for (int kb = 0; kb < nkb; ++kb, ++kg) {
+                int s = (int)(kg % a.stages);
+                uint32_t ph = (uint32_t)((kg / a.stages) & 1);
+                if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) break;
+                uint8_t* st = smem + (size_t)s * stage_bytes;
+                tc::mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
+                int kx = (kb0 + kb) * MK;
+                tc::tma_load_2d(st, &mAh, &full[s], kx, a_row);
+                tc::tma_load_2d(st + A_TILE_BYTES, &mAl, &full[s], kx, a_row);
+                if (MODE == MODE_TRANSFORM) {
+                    for (int r = 0; r < N; r += B_ROWS_PER_TMA) {
+                        tc::tma_load_2d(st + 2 * A_TILE_BYTES + r * MK * 2, &mBh, &full[s], kx, b_row + r);
+                        tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, &mBl, &full[s], kx, b_row + r);
+                    }
+                } else {
+                    tc::tma_load_2d(st + 2 * A_TILE_BYTES, &mBh, &full[s], kx, b_row);
+                    tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes, &mBl, &full[s], kx, b_row);
                 }
-            } else {
-                tc::tma_load_2d(st + 2 * A_TILE_BYTES, &mBh, &full[s], kx, b_row);
-                tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes, &mBl, &full[s], kx, b_row);
             }
         }
     } else if (threadIdx.x == 32) {
         // ---- MMA issuer
-        for (int kb = 0; kb < nkb; ++kb) {
-            int s = kb % a.stages;
-            uint32_t ph = (uint32_t)((kb / a.stages) & 1);
-            if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) break;
+        long kg = 0;
+        int it = 0;
+        for (int item = blockIdx.x; item < a.n_items && !*abort_flag; item += gridDim.x, ++it) {
+            int a_row, b_row, kb0, nkb, tile, split;
+            work_item<MODE>(a, item, a_row, b_row, kb0, nkb, tile, split);
+            const int buf = it % nbuf, use = it / nbuf;
+            if (use > 0 && !tc::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), abort_flag, a.err)) break;
             tc::tc_fence_after();
-            uint32_t st = tc::smem_u32(smem + (size_t)s * stage_bytes);
-            uint32_t aH = st, aL = st + A_TILE_BYTES, bH = st + 2 * A_TILE_BYTES, bL = bH + b_bytes;
-            bool neg = false;
-            if (MODE == MODE_CONTRACT) {
-                unsigned long long k = (unsigned long long)(kb0 + kb) * MK;
-                neg = (int)(k % (unsigned long long)a.nu_pad) >= a.npos_pad;
-            }
+            const uint32_t dcol = tmem + (uint32_t)(buf * N);
+            bool ok = true;
+            for (int kb = 0; kb < nkb; ++kb, ++kg) {
+                int s = (int)(kg % a.stages);
+                uint32_t ph = (uint32_t)((kg / a.stages) & 1);
+                if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                uint32_t st = tc::smem_u32(smem + (size_t)s * stage_bytes);
+                uint32_t aH = st, aL = st + A_TILE_BYTES, bH = st + 2 * A_TILE_BYTES, bL = bH + b_bytes;
+                bool neg = false;
+                if (MODE == MODE_CONTRACT) {
+                    unsigned long long k = (unsigned long long)(kb0 + kb) * MK;
+                    neg = (int)(k % (unsigned long long)a.nu_pad) >= a.npos_pad;
+                }
 #pragma unroll
-            for (int ks = 0; ks < MK / 16; ++ks) {
-                const uint32_t koff = ks * 32;  // 16 bf16 along k
+                for (int ks = 0; ks < MK / 16; ++ks) {
+                    const uint32_t koff = ks * 32;  // 16 bf16 along k
 #pragma unroll
-                for (int p = 0; p < 3; ++p) {  // hi*hi, hi*lo, lo*hi
-                    uint32_t aa = (p == 2 ? aL : aH) + koff;
-                    uint32_t bb = (p == 1 ? bL : bH) + koff;
-                    for (int nc = 0; nc < N; nc += 256) {
-                        int nn = min(256, N - nc);
-                        uint32_t acc = (kb | ks | p) != 0 ? 1u : 0u;
-                        tc::mma_bf16(tmem + (uint32_t)nc, tc::sdesc_kmajor_sw64(aa),
-                                     tc::sdesc_kmajor_sw64(bb + (uint32_t)nc * MK * 2), tc::idesc_bf16_f32(MM, nn, neg), acc);
+                    for (int p = 0; p < 3; ++p) {  // hi*hi, hi*lo, lo*hi
+                        uint32_t aa = (p == 2 ? aL : aH) + koff;
+                        uint32_t bb = (p == 1 ? bL : bH) + koff;
+                        for (int nc = 0; nc < N; nc += 256) {
+                            int nn = min(256, N - nc);
+                            uint32_t acc = (kb | ks | p) != 0 ? 1u : 0u;
+                            tc::mma_bf16(dcol + (uint32_t)nc, tc::sdesc_kmajor_sw64(aa),
+                                         tc::sdesc_kmajor_sw64(bb + (uint32_t)nc * MK * 2), tc::idesc_bf16_f32(MM, nn, neg),
+                                         acc);
+                        }
                     }
                 }
+                tc::mma_commit(&empty[s]);
             }
-            tc::mma_commit(&empty[s]);
+            tc::mma_commit(&tfull[buf]);
+            if (!ok) break;
         }
-        tc::mma_commit(accb);
-    }
-    __syncwarp();
-
-    // ---- epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
-    bool ok = tc::mbar_wait(accb, 0, abort_flag, a.err);
-    __syncwarp();
-    tc::tc_fence_after();
-    if (ok && !*abort_flag && nkb > 0) {
-        const int r = warp * 32 + (threadIdx.x % 32);
-        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-        if (MODE == MODE_TRANSFORM) {
-            size_t grow = (size_t)a_row + r;
-            size_t Q = grow / a.nbf_p, m = grow % a.nbf_p;
-            size_t base = m * a.kdim + Q * a.nu_pad + a.n_off;
-            for (int c0 = 0; c0 < N; c0 += 16) {
-                uint32_t v[16];
-                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
-                uint32_t hi[8], lo[8];
+    } else if (warp >= 2) {
+        // ---- epilogue
+        const int r = (warp % 4) * 32 + (threadIdx.x % 32);
+        const uint32_t lane_base = tmem + ((uint32_t)((warp % 4) * 32) << 16);
+        int it = 0;
+        for (int item = blockIdx.x; item < a.n_items; item += gridDim.x, ++it) {
+            int a_row, b_row, kb0, nkb, tile, split;
+            work_item<MODE>(a, item, a_row, b_row, kb0, nkb, tile, split);
+            const int buf = it % nbuf, use = it / nbuf;
+            bool ok = tc::mbar_wait(&tfull[buf], (uint32_t)(use & 1), abort_flag, a.err);
+            __syncwarp();
+            if (!ok || *abort_flag) break;
+            tc::tc_fence_after();
+            const uint32_t cbase = lane_base + (uint32_t)(buf * N);
+            if (MODE == MODE_TRANSFORM) {
+                size_t grow = (size_t)a_row + r;
+                size_t Q = grow / a.nbf_p, m = grow % a.nbf_p;
+                size_t base = m * a.kdim + Q * a.nu_pad + a.n_off;
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    uint32_t v[16];
+                    tc::tmem_ld16(cbase + (uint32_t)c0, v);
+                    uint32_t hi[8], lo[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    float x0 = __uint_as_float(v[2 * j]), x1 = __uint_as_float(v[2 * j + 1]);
-                    __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-                    hi[j] = pack_bf162(__bfloat162float(h0), __bfloat162float(h1));
-                    lo[j] = pack_bf162(x0 - __bfloat162float(h0), x1 - __bfloat162float(h1));
+                    for (int j = 0; j < 8; ++j) {
+                        float x0 = __uint_as_float(v[2 * j]), x1 = __uint_as_float(v[2 * j + 1]);
+                        __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+                        hi[j] = pack_bf162(__bfloat162float(h0), __bfloat162float(h1));
+                        lo[j] = pack_bf162(x0 - __bfloat162float(h0), x1 - __bfloat162float(h1));
+                    }
+                    uint4* dh = reinterpret_cast<uint4*>(a.Xhi + base + c0);
+                    uint4* dl = reinterpret_cast<uint4*>(a.Xlo + base + c0);
+                    dh[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                    dh[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
+                    dl[0] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                    dl[1] = make_uint4(lo[4], lo[5], lo[6], lo[7]);
                 }
-                uint4* dh = reinterpret_cast<uint4*>(a.Xhi + base + c0);
-                uint4* dl = reinterpret_cast<uint4*>(a.Xlo + base + c0);
-                dh[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-                dh[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
-                dl[0] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-                dl[1] = make_uint4(lo[4], lo[5], lo[6], lo[7]);
-            }
-        } else {
-            float* dst = a.part + (((size_t)split * a.ntiles_out + tile) * MM + r) * MM;
-            for (int c0 = 0; c0 < MM; c0 += 16) {
-                uint32_t v[16];
-                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
-                float4* d4 = reinterpret_cast<float4*>(dst + c0);
+            } else {
+                float* dst = a.part + (((size_t)split * a.ntiles_out + tile) * MM + r) * MM;
+                for (int c0 = 0; c0 < MM; c0 += 16) {
+                    uint32_t v[16];
+                    tc::tmem_ld16(cbase + (uint32_t)c0, v);
+                    float4* d4 = reinterpret_cast<float4*>(dst + c0);
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    d4[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
-                                        __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+                    for (int j = 0; j < 4; ++j)
+                        d4[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                                            __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+                }
             }
+            tc::tc_fence_before();
+            __syncwarp();
+            if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[buf]);
         }
     }
+    __syncwarp();
     if (*abort_flag && threadIdx.x == 0) {
         // let copies already issued land before the block's shared memory goes away
         uint64_t t0 = tc::global_timer();
@@ -360,6 +409,7 @@ struct MixedState {
     bool have_prev = false;
     int* err = nullptr;
     bool attrs_set = false;
+    int num_sms = 0;
 };
 
 MixedState* mixed_create() { return new MixedState(); }
@@ -457,6 +507,12 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         int blocks = (int)std::min<size_t>((ue + 255) / 256, 152 * 16);
         split_Ut_kernel<<<blocks, 256, 0, s>>>(U, ldu, nbf, npos, nneg, npos_pad, nu_pad, nbf_p, m->Uh, m->Ul);
     }
+    if (!m->num_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (m->num_sms <= 0) m->num_sms = 152;
+    }
     if (!m->attrs_set) {
         cudaFuncSetAttribute(tc_gemm_kernel<MODE_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
         cudaFuncSetAttribute(tc_gemm_kernel<MODE_CONTRACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
@@ -484,16 +540,21 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         ta.err = m->err;
         int stage_bytes = 2 * A_TILE_BYTES + 2 * ta.n_cols * MK * 2;
         ta.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / stage_bytes);
-        ta.tmem_cols = pow2_cols(ta.n_cols);
-        unsigned grid = (unsigned)((size_t)naux * nbf_p / MM);
-        tc_gemm_kernel<MODE_TRANSFORM><<<grid, 128, SMEM_BUDGET, s>>>(mBh, mBl, mUh, mUl, ta);
+        ta.nbuf = (2 * ta.n_cols <= 512) ? 2 : 1;
+        ta.tmem_cols = pow2_cols(ta.nbuf * ta.n_cols);
+        ta.n_items = (int)((size_t)naux * nbf_p / MM);
+        unsigned grid = (unsigned)std::min(ta.n_items, m->num_sms);
+        tc_gemm_kernel<MODE_TRANSFORM><<<grid, TC_THREADS, SMEM_BUDGET, s>>>(mBh, mBl, mUh, mUl, ta);
     }
     if (ev_transform_done) cudaEventRecord(ev_transform_done, s);
     // ---- contraction
     const int ntr = nbf_p / MM;
     const int ntiles_out = ntr * (ntr + 1) / 2;
     const int nkb_total = (int)(kdim / MK);
-    int nsplit = std::max(1, (152 * 2 + ntiles_out - 1) / ntiles_out);
+    // at least ~8 work items per SM, and at most 256 k blocks (8192 terms) per FP32
+    // accumulation run so the accumulation error stays below the BF16x3 splitting error
+    int nsplit = std::max(1, (m->num_sms * 8 + ntiles_out - 1) / ntiles_out);
+    nsplit = std::max(nsplit, (nkb_total + 255) / 256);
     nsplit = std::min(nsplit, std::max(1, nkb_total / 16));
     int kb_per_split = (nkb_total + nsplit - 1) / nsplit;
     nsplit = (nkb_total + kb_per_split - 1) / kb_per_split;
@@ -515,9 +576,11 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
     ca.part = m->part;
     ca.err = m->err;
     ca.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / (4 * A_TILE_BYTES));
-    ca.tmem_cols = MM;
-    dim3 cgrid(ntiles_out, nsplit);
-    tc_gemm_kernel<MODE_CONTRACT><<<cgrid, 128, SMEM_BUDGET, s>>>(mXh, mXl, mXh, mXl, ca);
+    ca.nbuf = 2;
+    ca.tmem_cols = pow2_cols(2 * MM);
+    ca.n_items = ntiles_out * nsplit;
+    unsigned cgrid = (unsigned)std::min(ca.n_items, m->num_sms);
+    tc_gemm_kernel<MODE_CONTRACT><<<cgrid, TC_THREADS, SMEM_BUDGET, s>>>(mXh, mXl, mXh, mXl, ca);
     // ---- fixed-order FP64 reduction (+ running K for incremental builds)
     size_t kn = (size_t)nbf * nbf;
     if (kn > m->Kacc_cap) {

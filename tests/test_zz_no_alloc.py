@@ -17,7 +17,7 @@ from psi4_gb300.jk import DFJKEngine
 from tests.helpers import random_orbitals, system
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-10
+TOL = 1e-10  # plus 1e-14 of max|J|: random orbitals drive J far above physical magnitudes
 
 
 def _noalloc(L, nbf, naux, B, D, J, stream):
@@ -43,7 +43,7 @@ def test_noalloc_matches_regular_entry_point(ints_built, jk_built, case):
         assert rc == 0, L.gdfjk_last_error(None).decode()
         torch.cuda.synchronize()
         Jref, _, _ = eng.compute(C, mode=abi.DO_J)
-        assert np.abs(J.cpu().numpy() - Jref).max() < TOL
+        assert np.abs(J.cpu().numpy() - Jref).max() < TOL + 1e-14 * np.abs(Jref).max()
 
 
 def test_noalloc_rejects_oversized_naux(jk_built):
