@@ -11,19 +11,20 @@
 //   contraction     K[m][n] = sum_{Q,j} s_j X[m][Q,j] X[n][Q,j]   lower 128x128 tiles, split-K
 //
 // The B operand of the half-transform (dense, both triangles, BF16 hi/lo) is built once from
-// the FP64 tiles.  Operand tiles arrive by TMA (64-byte swizzle, 32 k per stage) into a
-// multi-stage shared-memory ring guarded by mbarriers; one thread issues tcgen05.mma, four
-// warps drain the accumulator with tcgen05.ld.  The negative k-blocks of an incremental
+// the FP64 tiles.  Every operand lives in HBM pre-swizzled, in contiguous blocks that are the
+// exact shared-memory image of one 64-byte-swizzled K-major tile (128 or 64 rows x 32 k), so
+// the producer moves each tile with a single cp.async.bulk (TMA bulk copy) into a multi-stage
+// ring guarded by mbarriers; the transform's epilogue writes X in that same blocked form.
+// One thread issues tcgen05.mma; four warps drain the TMEM accumulators with tcgen05.ld.  The negative k-blocks of an incremental
 // build use the instruction's negate-A bit.  Split-K partials (FP32) are summed in FP64 in
 // a fixed order, so repeated builds are bitwise identical.
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "gdfjk.h"
 #include "mixed.cuh"
@@ -35,6 +36,7 @@ constexpr int MM = 128;                    // tile rows (MMA M)
 constexpr int MK = 32;                     // k per pipeline stage: one 64-byte swizzle row of bf16
 constexpr int A_TILE_BYTES = MM * MK * 2;  // 8 KB
 constexpr int B_ROWS_PER_TMA = 64;
+constexpr int CN = 256;                    // contraction tile columns (MMA N)
 constexpr int SMEM_BUDGET = 224 * 1024;
 constexpr int SMEM_RESERVE = 2048;         // alignment slack + barriers
 
@@ -56,17 +58,16 @@ struct TcArgs {
     float* part;
     int stages;
     int tmem_cols;
+    const int2* tiles;  // contraction: (row block of 128, column block of 256) covering the lower triangle
+    const __nv_bfloat16* zero_blk;  // 8 KB of zeros (operand rows past the end)
+    const __nv_bfloat16* Bsh;       // transform operands, pre-swizzled blocks
+    const __nv_bfloat16* Bsl;
+    const __nv_bfloat16* Uth;
+    const __nv_bfloat16* Utl;
     int n_items;  // work items of this launch
     int nbuf;     // TMEM accumulators (2 overlaps the epilogue with the next item)
     int* err;
 };
-
-__device__ __forceinline__ void tile_of(int t, int& I, int& J) {
-    I = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
-    while (I * (I + 1) / 2 > t) --I;
-    while ((I + 1) * (I + 2) / 2 <= t) ++I;
-    J = t - I * (I + 1) / 2;
-}
 
 __device__ __forceinline__ uint32_t pack_bf162(float a, float b) {
     __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
@@ -93,20 +94,16 @@ __device__ __forceinline__ void work_item(const TcArgs& a, int item, int& a_row,
     } else {
         split = item / a.ntiles_out;  // split-major: concurrent CTAs share one k window in L2
         tile = item % a.ntiles_out;
-        int I, J;
-        tile_of(tile, I, J);
-        a_row = I * MM;
-        b_row = J * MM;
+        int2 ij = a.tiles[tile];
+        a_row = ij.x * MM;
+        b_row = ij.y * CN;
         kb0 = split * a.kb_per_split;
         nkb = min(a.kb_per_split, a.nkb_total - kb0);
     }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mAh,
-                                                                const __grid_constant__ CUtensorMap mAl,
-                                                                const __grid_constant__ CUtensorMap mBh,
-                                                                const __grid_constant__ CUtensorMap mBl, const TcArgs a) {
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int N = a.n_cols;
@@ -132,10 +129,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const __grid_con
         }
         *abort_flag = 0;
         tc::fence_barrier_init();
-        tc::prefetch_tmap(&mAh);
-        tc::prefetch_tmap(&mAl);
-        tc::prefetch_tmap(&mBh);
-        tc::prefetch_tmap(&mBl);
     }
     if (warp == 0) tc::tmem_alloc(tmem_holder, (uint32_t)a.tmem_cols);
     tc::tc_fence_before();
@@ -155,17 +148,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const __grid_con
                 if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) break;
                 uint8_t* st = smem + (size_t)s * stage_bytes;
                 tc::mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
-                int kx = (kb0 + kb) * MK;
-                tc::tma_load_2d(st, &mAh, &full[s], kx, a_row);
-                tc::tma_load_2d(st + A_TILE_BYTES, &mAl, &full[s], kx, a_row);
+                const size_t kbg = (size_t)(kb0 + kb);
                 if (MODE == MODE_TRANSFORM) {
+                    // B slices (8 KB blocks, 128 rows) and U^T slices (4 KB blocks, 64 rows)
+                    const size_t nkbB = a.nbf_p / MK;
+                    const size_t ba = ((size_t)(a_row / MM) * nkbB + kbg) * (MM * MK);
+                    tc::bulk_load(st, a.Bsh + ba, A_TILE_BYTES, &full[s]);
+                    tc::bulk_load(st + A_TILE_BYTES, a.Bsl + ba, A_TILE_BYTES, &full[s]);
                     for (int r = 0; r < N; r += B_ROWS_PER_TMA) {
-                        tc::tma_load_2d(st + 2 * A_TILE_BYTES + r * MK * 2, &mBh, &full[s], kx, b_row + r);
-                        tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, &mBl, &full[s], kx, b_row + r);
+                        const size_t bu = ((size_t)((b_row + r) / B_ROWS_PER_TMA) * nkbB + kbg) * (B_ROWS_PER_TMA * MK);
+                        tc::bulk_load(st + 2 * A_TILE_BYTES + r * MK * 2, a.Uth + bu, B_ROWS_PER_TMA * MK * 2, &full[s]);
+                        tc::bulk_load(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, a.Utl + bu, B_ROWS_PER_TMA * MK * 2,
+                                      &full[s]);
                     }
                 } else {
-                    tc::tma_load_2d(st + 2 * A_TILE_BYTES, &mBh, &full[s], kx, b_row);
-                    tc::tma_load_2d(st + 2 * A_TILE_BYTES + b_bytes, &mBl, &full[s], kx, b_row);
+                    // X slices (8 KB blocks); rows past the end come from a zero block
+                    const size_t nkbt = a.kdim / MK;
+                    const size_t ba = ((size_t)(a_row / MM) * nkbt + kbg) * (MM * MK);
+                    tc::bulk_load(st, a.Xhi + ba, A_TILE_BYTES, &full[s]);
+                    tc::bulk_load(st + A_TILE_BYTES, a.Xlo + ba, A_TILE_BYTES, &full[s]);
+                    for (int r = 0; r < N; r += MM) {
+                        int rb = (b_row + r) / MM;
+                        const __nv_bfloat16* srch = a.zero_blk;
+                        const __nv_bfloat16* srcl = a.zero_blk;
+                        if (rb < a.nbf_p / MM) {
+                            const size_t bb = ((size_t)rb * nkbt + kbg) * (MM * MK);
+                            srch = a.Xhi + bb;
+                            srcl = a.Xlo + bb;
+                        }
+                        tc::bulk_load(st + 2 * A_TILE_BYTES + r * MK * 2, srch, A_TILE_BYTES, &full[s]);
+                        tc::bulk_load(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, srcl, A_TILE_BYTES, &full[s]);
+                    }
                 }
             }
         }
@@ -234,7 +247,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const __grid_con
             if (MODE == MODE_TRANSFORM) {
                 size_t grow = (size_t)a_row + r;
                 size_t Q = grow / a.nbf_p, m = grow % a.nbf_p;
-                size_t base = m * a.kdim + Q * a.nu_pad + a.n_off;
+                // X goes out pre-swizzled in 8 KB blocks (128 rows x 32 k): exactly the
+                // shared-memory image of one contraction operand tile
+                const size_t nkbt = a.kdim / MK;
+                const size_t rowblk = (m / MM) * nkbt;
+                const uint32_t rr = (uint32_t)(m % MM);
                 for (int c0 = 0; c0 < N; c0 += 16) {
                     uint32_t v[16];
                     tc::tmem_ld16(cbase + (uint32_t)c0, v);
@@ -246,16 +263,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const __grid_con
                         hi[j] = pack_bf162(__bfloat162float(h0), __bfloat162float(h1));
                         lo[j] = pack_bf162(x0 - __bfloat162float(h0), x1 - __bfloat162float(h1));
                     }
-                    uint4* dh = reinterpret_cast<uint4*>(a.Xhi + base + c0);
-                    uint4* dl = reinterpret_cast<uint4*>(a.Xlo + base + c0);
-                    dh[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-                    dh[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
-                    dl[0] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-                    dl[1] = make_uint4(lo[4], lo[5], lo[6], lo[7]);
+                    size_t k0 = Q * a.nu_pad + a.n_off + c0;
+                    size_t blk = (rowblk + k0 / MK) * (size_t)(MM * MK);  // elements
+                    uint32_t ch = (uint32_t)((k0 % MK) / 8);
+                    uint32_t o0 = tc::sw64_offset(rr, ch) / 2, o1 = tc::sw64_offset(rr, ch + 1) / 2;
+                    *reinterpret_cast<uint4*>(a.Xhi + blk + o0) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<uint4*>(a.Xhi + blk + o1) = make_uint4(hi[4], hi[5], hi[6], hi[7]);
+                    *reinterpret_cast<uint4*>(a.Xlo + blk + o0) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                    *reinterpret_cast<uint4*>(a.Xlo + blk + o1) = make_uint4(lo[4], lo[5], lo[6], lo[7]);
                 }
             } else {
-                float* dst = a.part + (((size_t)split * a.ntiles_out + tile) * MM + r) * MM;
-                for (int c0 = 0; c0 < MM; c0 += 16) {
+                float* dst = a.part + (((size_t)split * a.ntiles_out + tile) * MM + r) * CN;
+                for (int c0 = 0; c0 < CN; c0 += 16) {
                     uint32_t v[16];
                     tc::tmem_ld16(cbase + (uint32_t)c0, v);
                     float4* d4 = reinterpret_cast<float4*>(dst + c0);
@@ -301,8 +320,11 @@ __global__ void split_B_kernel(const double* __restrict__ B, int naux, int nbf, 
             }
         }
         __nv_bfloat16 h = __double2bfloat16(v);
-        Bh[row * nbf_p + n] = h;
-        Bl[row * nbf_p + n] = __double2bfloat16(v - (double)__bfloat162float(h));
+        // pre-swizzled 8 KB blocks (128 rows x 32 k): the shared-memory image of an operand tile
+        size_t blk = ((row / MM) * (size_t)(nbf_p / MK) + (size_t)(n / MK)) * (MM * MK);
+        size_t off = blk + tc::sw64_offset((uint32_t)(row % MM), (uint32_t)((n % MK) / 8)) / 2 + (n % 8);
+        Bh[off] = h;
+        Bl[off] = __double2bfloat16(v - (double)__bfloat162float(h));
     }
 }
 
@@ -321,70 +343,42 @@ __global__ void split_Ut_kernel(const double* __restrict__ U, int ldu, int nbf, 
         }
         double v = (col >= 0 && k < nbf) ? U[(size_t)k * ldu + col] : 0.0;
         __nv_bfloat16 h = __double2bfloat16(v);
-        Uh[e] = h;
-        Ul[e] = __double2bfloat16(v - (double)__bfloat162float(h));
+        // pre-swizzled 4 KB blocks (64 rows x 32 k)
+        size_t blk = ((size_t)(j / B_ROWS_PER_TMA) * (size_t)(nbf_p / MK) + (size_t)(k / MK)) * (B_ROWS_PER_TMA * MK);
+        size_t off = blk + tc::sw64_offset((uint32_t)(j % B_ROWS_PER_TMA), (uint32_t)((k % MK) / 8)) / 2 + (k % 8);
+        Uh[off] = h;
+        Ul[off] = __double2bfloat16(v - (double)__bfloat162float(h));
     }
 }
 
-// K[m][n] (and its mirror) = sum over splits (fixed order, FP64) of the partial tiles.
+// K[m][n] (and its mirror), m >= n, = sum over splits (fixed order, FP64) of the partial
+// tiles; `tile_of_block[I * ncb + Jc]` maps a (row block, column block) to its tile index.
 __global__ void reduce_mixed_kernel(const float* __restrict__ part, int nsplit, int ntiles_out, int nbf,
-                                    double* __restrict__ K, int ldk, double* __restrict__ Kacc, int accumulate) {
-    int t = blockIdx.x;
-    int I, J;
-    tile_of(t, I, J);
-    for (int e = threadIdx.x; e < MM * MM; e += blockDim.x) {
-        int r = e / MM, c = e % MM;
-        int m = I * MM + r, n = J * MM + c;
-        if (m >= nbf || n >= nbf) continue;
-        if (I == J && m < n) continue;  // the diagonal tile's upper half comes from its lower
+                                    const int* __restrict__ tile_of_block, int ncb, double* __restrict__ K, int ldk,
+                                    double* __restrict__ Kacc, int accumulate) {
+    size_t n_lower = (size_t)nbf * (nbf + 1) / 2;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n_lower; p += (size_t)gridDim.x * blockDim.x) {
+        size_t m = (size_t)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+        while (m * (m + 1) / 2 > p) --m;
+        while ((m + 1) * (m + 2) / 2 <= p) ++m;
+        size_t n = p - m * (m + 1) / 2;
+        int I = (int)(m / MM), Jc = (int)(n / CN);
+        int t = tile_of_block[I * ncb + Jc];
+        size_t off = ((size_t)t * MM + (m % MM)) * CN + (n % CN);
         double s = 0.0;
-        for (int k = 0; k < nsplit; ++k) s += (double)part[(((size_t)k * ntiles_out + t) * MM + r) * MM + c];
-        if (I == J && m > n) {
-            // symmetrise the diagonal tile
-            double s2 = 0.0;
-            for (int k = 0; k < nsplit; ++k) s2 += (double)part[(((size_t)k * ntiles_out + t) * MM + c) * MM + r];
-            s = 0.5 * (s + s2);
-        }
-        if (accumulate) {
-            s += Kacc[(size_t)m * nbf + n];
-        }
+        for (int k = 0; k < nsplit; ++k) s += (double)part[(size_t)k * ntiles_out * MM * CN + off];
+        if (accumulate) s += Kacc[m * nbf + n];
         if (Kacc) {
-            Kacc[(size_t)m * nbf + n] = s;
-            Kacc[(size_t)n * nbf + m] = s;
+            Kacc[m * nbf + n] = s;
+            Kacc[n * nbf + m] = s;
         }
-        K[(size_t)m * ldk + n] = s;
-        K[(size_t)n * ldk + m] = s;
+        K[m * ldk + n] = s;
+        K[n * ldk + m] = s;
     }
 }
 
 // ---------------------------------------------------------------- host side
 namespace {
-
-PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
-
-// 2D bf16 tensor [rows][cols] (cols contiguous), box {32, box_rows}, 64-byte swizzle.
-bool make_map(CUtensorMap* m, const void* base, unsigned long long cols, unsigned long long rows, int box_rows) {
-    auto enc = get_encode();
-    if (!enc) return false;
-    cuuint64_t dims[2] = {cols, rows};
-    cuuint64_t strides[1] = {cols * 2};
-    cuuint32_t box[2] = {(cuuint32_t)MK, (cuuint32_t)box_rows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
 
 int pow2_cols(int n) {
     int c = 32;
@@ -410,18 +404,27 @@ struct MixedState {
     int* err = nullptr;
     bool attrs_set = false;
     int num_sms = 0;
+    int2* d_tiles = nullptr;
+    int* d_tile_of_block = nullptr;
+    int tiles_nbf_p = 0, ntiles_c = 0, ncb = 0;
+    __nv_bfloat16* zero_blk = nullptr;
 };
 
 MixedState* mixed_create() { return new MixedState(); }
 
 static void free_all(MixedState* m) {
-    void* ps[] = {m->Bh, m->Bl, m->Uh, m->Ul, m->Xh, m->Xl, m->part, m->Kacc, m->err};
+    void* ps[] = {m->Bh, m->Bl, m->Uh, m->Ul, m->Xh, m->Xl, m->part, m->Kacc, m->err, m->d_tiles, m->d_tile_of_block,
+                  m->zero_blk};
     for (void* p : ps)
         if (p) cudaFree(p);
     m->Bh = m->Bl = m->Uh = m->Ul = m->Xh = m->Xl = nullptr;
     m->part = nullptr;
     m->Kacc = nullptr;
     m->err = nullptr;
+    m->d_tiles = nullptr;
+    m->d_tile_of_block = nullptr;
+    m->zero_blk = nullptr;
+    m->tiles_nbf_p = 0;
     m->U_cap = m->X_cap = m->part_cap = m->Kacc_cap = 0;
     m->B_ready = false;
     m->have_prev = false;
@@ -476,6 +479,10 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         if ((rc = dalloc_bytes((void**)&m->err, sizeof(int), err))) return rc;
         cudaMemsetAsync(m->err, 0, sizeof(int), s);
     }
+    if (!m->zero_blk) {
+        if ((rc = dalloc_bytes((void**)&m->zero_blk, A_TILE_BYTES, err))) return rc;
+        cudaMemsetAsync(m->zero_blk, 0, A_TILE_BYTES, s);
+    }
     if (!m->B_ready || m->nbf_p != nbf_p) {
         size_t bytes = (size_t)naux * nbf_p * nbf_p * 2;
         if ((rc = dalloc_bytes((void**)&m->Bh, bytes, err)) || (rc = dalloc_bytes((void**)&m->Bl, bytes, err))) return rc;
@@ -519,14 +526,6 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         m->attrs_set = true;
     }
     // ---- half-transform, in accumulator chunks of at most 448 columns
-    CUtensorMap mBh, mBl, mUh, mUl, mXh, mXl;
-    if (!make_map(&mBh, m->Bh, nbf_p, (unsigned long long)naux * nbf_p, MM) ||
-        !make_map(&mBl, m->Bl, nbf_p, (unsigned long long)naux * nbf_p, MM) ||
-        !make_map(&mUh, m->Uh, nbf_p, nu_pad, B_ROWS_PER_TMA) || !make_map(&mUl, m->Ul, nbf_p, nu_pad, B_ROWS_PER_TMA) ||
-        !make_map(&mXh, m->Xh, kdim, nbf_p, MM) || !make_map(&mXl, m->Xl, kdim, nbf_p, MM)) {
-        err = "mixed: cuTensorMapEncodeTiled failed";
-        return GDFJK_ERR_CUDA;
-    }
     for (int n_off = 0; n_off < nu_pad; n_off += 448) {
         TcArgs ta{};
         ta.nbf_p = nbf_p;
@@ -538,18 +537,42 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         ta.Xhi = m->Xh;
         ta.Xlo = m->Xl;
         ta.err = m->err;
+        ta.tiles = nullptr;
+        ta.zero_blk = nullptr;
+        ta.Bsh = m->Bh;
+        ta.Bsl = m->Bl;
+        ta.Uth = m->Uh;
+        ta.Utl = m->Ul;
         int stage_bytes = 2 * A_TILE_BYTES + 2 * ta.n_cols * MK * 2;
         ta.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / stage_bytes);
         ta.nbuf = (2 * ta.n_cols <= 512) ? 2 : 1;
         ta.tmem_cols = pow2_cols(ta.nbuf * ta.n_cols);
         ta.n_items = (int)((size_t)naux * nbf_p / MM);
         unsigned grid = (unsigned)std::min(ta.n_items, m->num_sms);
-        tc_gemm_kernel<MODE_TRANSFORM><<<grid, TC_THREADS, SMEM_BUDGET, s>>>(mBh, mBl, mUh, mUl, ta);
+        tc_gemm_kernel<MODE_TRANSFORM><<<grid, TC_THREADS, SMEM_BUDGET, s>>>(ta);
     }
     if (ev_transform_done) cudaEventRecord(ev_transform_done, s);
-    // ---- contraction
+    // ---- contraction: 128 x 256 tiles covering the lower triangle
     const int ntr = nbf_p / MM;
-    const int ntiles_out = ntr * (ntr + 1) / 2;
+    if (m->tiles_nbf_p != nbf_p) {
+        const int ncb = (nbf_p + CN - 1) / CN;
+        std::vector<int2> tl;
+        std::vector<int> tob((size_t)ntr * ncb, -1);
+        for (int I = 0; I < ntr; ++I)
+            for (int Jc = 0; Jc < ncb && Jc * CN <= I * MM + MM - 1; ++Jc) {
+                tob[(size_t)I * ncb + Jc] = (int)tl.size();
+                tl.push_back(make_int2(I, Jc));
+            }
+        if ((rc = dalloc_bytes((void**)&m->d_tiles, tl.size() * sizeof(int2), err)) ||
+            (rc = dalloc_bytes((void**)&m->d_tile_of_block, tob.size() * sizeof(int), err)))
+            return rc;
+        cudaMemcpy(m->d_tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        cudaMemcpy(m->d_tile_of_block, tob.data(), tob.size() * sizeof(int), cudaMemcpyHostToDevice);
+        m->ntiles_c = (int)tl.size();
+        m->ncb = ncb;
+        m->tiles_nbf_p = nbf_p;
+    }
+    const int ntiles_out = m->ntiles_c;
     const int nkb_total = (int)(kdim / MK);
     // at least ~8 work items per SM, and at most 256 k blocks (8192 terms) per FP32
     // accumulation run so the accumulation error stays below the BF16x3 splitting error
@@ -558,7 +581,7 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
     nsplit = std::min(nsplit, std::max(1, nkb_total / 16));
     int kb_per_split = (nkb_total + nsplit - 1) / nsplit;
     nsplit = (nkb_total + kb_per_split - 1) / kb_per_split;
-    size_t pe = (size_t)nsplit * ntiles_out * MM * MM;
+    size_t pe = (size_t)nsplit * ntiles_out * MM * CN;
     if (pe > m->part_cap) {
         if ((rc = dalloc_bytes((void**)&m->part, pe * 4, err))) return rc;
         m->part_cap = pe;
@@ -567,7 +590,11 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
     ca.nbf_p = nbf_p;
     ca.nu_pad = nu_pad;
     ca.npos_pad = npos_pad;
-    ca.n_cols = MM;
+    ca.n_cols = CN;
+    ca.tiles = m->d_tiles;
+    ca.zero_blk = m->zero_blk;
+    ca.Xhi = m->Xh;
+    ca.Xlo = m->Xl;
     ca.kdim = kdim;
     ca.ntr = ntr;
     ca.kb_per_split = kb_per_split;
@@ -575,12 +602,12 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
     ca.ntiles_out = ntiles_out;
     ca.part = m->part;
     ca.err = m->err;
-    ca.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / (4 * A_TILE_BYTES));
+    ca.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / (2 * A_TILE_BYTES + 2 * CN * MK * 2));
     ca.nbuf = 2;
-    ca.tmem_cols = pow2_cols(2 * MM);
+    ca.tmem_cols = pow2_cols(2 * CN);
     ca.n_items = ntiles_out * nsplit;
     unsigned cgrid = (unsigned)std::min(ca.n_items, m->num_sms);
-    tc_gemm_kernel<MODE_CONTRACT><<<cgrid, TC_THREADS, SMEM_BUDGET, s>>>(mXh, mXl, mXh, mXl, ca);
+    tc_gemm_kernel<MODE_CONTRACT><<<cgrid, TC_THREADS, SMEM_BUDGET, s>>>(ca);
     // ---- fixed-order FP64 reduction (+ running K for incremental builds)
     size_t kn = (size_t)nbf * nbf;
     if (kn > m->Kacc_cap) {
@@ -589,7 +616,12 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         m->have_prev = false;
     }
     int acc = (accumulate && m->have_prev) ? 1 : 0;
-    reduce_mixed_kernel<<<ntiles_out, 256, 0, s>>>(m->part, nsplit, ntiles_out, nbf, K, nbf, m->Kacc, acc);
+    {
+        size_t nl = (size_t)nbf * (nbf + 1) / 2;
+        int blocks = (int)std::min<size_t>((nl + 255) / 256, (size_t)m->num_sms * 16);
+        reduce_mixed_kernel<<<blocks, 256, 0, s>>>(m->part, nsplit, ntiles_out, nbf, m->d_tile_of_block, m->ncb, K, nbf,
+                                                   m->Kacc, acc);
+    }
     m->have_prev = true;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -76,6 +76,21 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+// 1D bulk copy global -> this CTA's shared memory (16-byte aligned, size a multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Byte offset of (row r, 16-byte chunk c) inside a K-major operand tile with 64-byte rows and
+// the 64-byte swizzle (chunk index XOR bits 1-2 of the row): the layout TMA's
+// CU_TENSOR_MAP_SWIZZLE_64B writes and the sdesc_kmajor_sw64 descriptor reads.
+__host__ __device__ __forceinline__ uint32_t sw64_offset(uint32_t r, uint32_t c) {
+    return r * 64u + ((c ^ ((r >> 1) & 3u)) << 4);
+}
+
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
