@@ -33,9 +33,9 @@
 namespace gdfjk {
 
 constexpr int MM = 128;                    // tile rows (MMA M)
-constexpr int MK = 32;                     // k per pipeline stage: one 64-byte swizzle row of bf16
+constexpr int MK = tc::SWZ / 2;            // k per pipeline stage: one swizzle row of bf16
 constexpr int A_TILE_BYTES = MM * MK * 2;  // 8 KB
-constexpr int B_ROWS_PER_TMA = 64;
+constexpr int U_ROW_ALIGN = 32;            // U^T column groups are padded to 32 rows
 constexpr int CN = 256;                    // contraction tile columns (MMA N)
 constexpr int SMEM_BUDGET = 224 * 1024;
 constexpr int SMEM_RESERVE = 2048;         // alignment slack + barriers
@@ -45,7 +45,8 @@ enum { MODE_TRANSFORM = 0, MODE_CONTRACT = 1 };
 struct TcArgs {
     int nbf_p;        // padded nbf (multiple of 128)
     int nu_pad;       // columns of U (multiple of 64)
-    int npos_pad;     // positive columns (multiple of 64)
+    int npos_pad;     // positive columns (multiple of 32)
+    int n_mtiles;     // transform: 128-row tiles in total
     int n_cols;       // accumulator columns of this launch (transform) or 128 (contraction)
     int n_off;        // first U column of this launch (transform)
     unsigned long long kdim;  // naux * nu_pad
@@ -108,7 +109,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int N = a.n_cols;
     const int b_bytes = N * MK * 2;
-    const int stage_bytes = 2 * A_TILE_BYTES + 2 * b_bytes;
+    const int a_bytes = 2 * A_TILE_BYTES;  // hi/lo of the A tile
+    const int stage_bytes = a_bytes + 2 * b_bytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * stage_bytes);
     uint64_t* empty = full + a.stages;
     uint64_t* tfull = empty + a.stages;  // [2]
@@ -137,95 +139,121 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
     const uint32_t tmem = *tmem_holder;
 
     if (threadIdx.x == 0) {
-        // ---- TMA producer
+        // ---- producer: one bulk copy per operand slice per stage; stage/phase kept incrementally
+        int s = 0;
+        uint32_t ph = 0;
         long kg = 0;
+        const size_t blkA = (size_t)MM * MK;  // elements per 128-row operand block
         for (int item = blockIdx.x; item < a.n_items && !*abort_flag; item += gridDim.x) {
             int a_row, b_row, kb0, nkb, tile, split;
             work_item<MODE>(a, item, a_row, b_row, kb0, nkb, tile, split);
+            const __nv_bfloat16 *pah, *pal, *pbh, *pbl, *pch = nullptr, *pcl = nullptr;
+            size_t stepb;
+            if (MODE == MODE_TRANSFORM) {
+                const size_t nkbB = a.nbf_p / MK;
+                pah = a.Bsh + ((size_t)(a_row / MM) * nkbB + kb0) * blkA;
+                pal = a.Bsl + ((size_t)(a_row / MM) * nkbB + kb0) * blkA;
+                pbh = a.Uth + (size_t)kb0 * a.nu_pad * MK + (size_t)b_row * MK;
+                pbl = a.Utl + (size_t)kb0 * a.nu_pad * MK + (size_t)b_row * MK;
+                stepb = (size_t)a.nu_pad * MK;
+            } else {
+                const size_t nkbt = a.kdim / MK;
+                pah = a.Xhi + ((size_t)(a_row / MM) * nkbt + kb0) * blkA;
+                pal = a.Xlo + ((size_t)(a_row / MM) * nkbt + kb0) * blkA;
+                const int rb0 = b_row / MM, nrb = a.nbf_p / MM;
+                // the two 128-row halves of the 256-row B tile; rows past the end read zeros
+                pbh = rb0 < nrb ? a.Xhi + ((size_t)rb0 * nkbt + kb0) * blkA : a.zero_blk;
+                pbl = rb0 < nrb ? a.Xlo + ((size_t)rb0 * nkbt + kb0) * blkA : a.zero_blk;
+                pch = rb0 + 1 < nrb ? a.Xhi + ((size_t)(rb0 + 1) * nkbt + kb0) * blkA : a.zero_blk;
+                pcl = rb0 + 1 < nrb ? a.Xlo + ((size_t)(rb0 + 1) * nkbt + kb0) * blkA : a.zero_blk;
+                stepb = blkA;
+            }
+            const size_t stepc0 = (MODE == MODE_CONTRACT && (b_row / MM) < a.nbf_p / MM) ? blkA : 0;
+            const size_t stepc1 = (MODE == MODE_CONTRACT && (b_row / MM) + 1 < a.nbf_p / MM) ? blkA : 0;
             for (int kb = 0; kb < nkb; ++kb, ++kg) {
-                int s = (int)(kg % a.stages);
-                uint32_t ph = (uint32_t)((kg / a.stages) & 1);
                 if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) break;
                 uint8_t* st = smem + (size_t)s * stage_bytes;
                 tc::mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
-                const size_t kbg = (size_t)(kb0 + kb);
+                tc::bulk_load(st, pah, A_TILE_BYTES, &full[s]);
+                tc::bulk_load(st + A_TILE_BYTES, pal, A_TILE_BYTES, &full[s]);
+                pah += blkA;
+                pal += blkA;
                 if (MODE == MODE_TRANSFORM) {
-                    // B slices (8 KB blocks, 128 rows) and U^T slices (4 KB blocks, 64 rows)
-                    const size_t nkbB = a.nbf_p / MK;
-                    const size_t ba = ((size_t)(a_row / MM) * nkbB + kbg) * (MM * MK);
-                    tc::bulk_load(st, a.Bsh + ba, A_TILE_BYTES, &full[s]);
-                    tc::bulk_load(st + A_TILE_BYTES, a.Bsl + ba, A_TILE_BYTES, &full[s]);
-                    for (int r = 0; r < N; r += B_ROWS_PER_TMA) {
-                        const size_t bu = ((size_t)((b_row + r) / B_ROWS_PER_TMA) * nkbB + kbg) * (B_ROWS_PER_TMA * MK);
-                        tc::bulk_load(st + 2 * A_TILE_BYTES + r * MK * 2, a.Uth + bu, B_ROWS_PER_TMA * MK * 2, &full[s]);
-                        tc::bulk_load(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, a.Utl + bu, B_ROWS_PER_TMA * MK * 2,
-                                      &full[s]);
-                    }
+                    tc::bulk_load(st + a_bytes, pbh, (uint32_t)b_bytes, &full[s]);
+                    tc::bulk_load(st + a_bytes + b_bytes, pbl, (uint32_t)b_bytes, &full[s]);
+                    pbh += stepb;
+                    pbl += stepb;
                 } else {
-                    // X slices (8 KB blocks); rows past the end come from a zero block
-                    const size_t nkbt = a.kdim / MK;
-                    const size_t ba = ((size_t)(a_row / MM) * nkbt + kbg) * (MM * MK);
-                    tc::bulk_load(st, a.Xhi + ba, A_TILE_BYTES, &full[s]);
-                    tc::bulk_load(st + A_TILE_BYTES, a.Xlo + ba, A_TILE_BYTES, &full[s]);
-                    for (int r = 0; r < N; r += MM) {
-                        int rb = (b_row + r) / MM;
-                        const __nv_bfloat16* srch = a.zero_blk;
-                        const __nv_bfloat16* srcl = a.zero_blk;
-                        if (rb < a.nbf_p / MM) {
-                            const size_t bb = ((size_t)rb * nkbt + kbg) * (MM * MK);
-                            srch = a.Xhi + bb;
-                            srcl = a.Xlo + bb;
-                        }
-                        tc::bulk_load(st + 2 * A_TILE_BYTES + r * MK * 2, srch, A_TILE_BYTES, &full[s]);
-                        tc::bulk_load(st + 2 * A_TILE_BYTES + b_bytes + r * MK * 2, srcl, A_TILE_BYTES, &full[s]);
-                    }
+                    tc::bulk_load(st + a_bytes, pbh, A_TILE_BYTES, &full[s]);
+                    tc::bulk_load(st + a_bytes + A_TILE_BYTES, pch, A_TILE_BYTES, &full[s]);
+                    tc::bulk_load(st + a_bytes + b_bytes, pbl, A_TILE_BYTES, &full[s]);
+                    tc::bulk_load(st + a_bytes + b_bytes + A_TILE_BYTES, pcl, A_TILE_BYTES, &full[s]);
+                    pbh += stepc0;
+                    pbl += stepc0;
+                    pch += stepc1;
+                    pcl += stepc1;
+                }
+                if (++s == a.stages) {
+                    s = 0;
+                    ph ^= 1u;
                 }
             }
         }
     } else if (threadIdx.x == 32) {
-        // ---- MMA issuer
-        long kg = 0;
+        // ---- MMA issuer: descriptors built once per stage and advanced by constants along k
+        int s = 0;
+        uint32_t ph = 0;
         int it = 0;
+        const uint32_t smem_base = tc::smem_u32(smem);
+        const int n1 = N < 256 ? N : 256;
+        const int n2 = N - n1;  // second MMA of a row when N > 256
+        const uint32_t id1p = tc::idesc_bf16_f32(MM, n1, false), id1n = tc::idesc_bf16_f32(MM, n1, true);
+        const uint32_t id2p = n2 > 0 ? tc::idesc_bf16_f32(MM, n2, false) : 0u;
+        const uint32_t id2n = n2 > 0 ? tc::idesc_bf16_f32(MM, n2, true) : 0u;
+        const uint64_t boff2 = (uint64_t)((256 * MK * 2) >> 4);  // second N chunk inside the B tile
         for (int item = blockIdx.x; item < a.n_items && !*abort_flag; item += gridDim.x, ++it) {
             int a_row, b_row, kb0, nkb, tile, split;
             work_item<MODE>(a, item, a_row, b_row, kb0, nkb, tile, split);
             const int buf = it % nbuf, use = it / nbuf;
             if (use > 0 && !tc::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), abort_flag, a.err)) break;
             tc::tc_fence_after();
-            const uint32_t dcol = tmem + (uint32_t)(buf * N);
+            const uint32_t d1 = tmem + (uint32_t)(buf * N), d2 = d1 + 256u;
+            // position of the first k block inside its group of nu_pad columns (sign of dD)
+            int kmod = (MODE == MODE_CONTRACT) ? (int)(((unsigned long long)kb0 * MK) % (unsigned long long)a.nu_pad) : 0;
             bool ok = true;
-            for (int kb = 0; kb < nkb; ++kb, ++kg) {
-                int s = (int)(kg % a.stages);
-                uint32_t ph = (uint32_t)((kg / a.stages) & 1);
+            for (int kb = 0; kb < nkb; ++kb) {
                 if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
                     ok = false;
                     break;
                 }
                 tc::tc_fence_after();
-                uint32_t st = tc::smem_u32(smem + (size_t)s * stage_bytes);
-                uint32_t aH = st, aL = st + A_TILE_BYTES, bH = st + 2 * A_TILE_BYTES, bL = bH + b_bytes;
+                const uint32_t st = smem_base + (uint32_t)(s * stage_bytes);
+                const uint64_t dAh = tc::sdesc_kmajor(st), dAl = tc::sdesc_kmajor(st + A_TILE_BYTES);
+                const uint64_t dBh = tc::sdesc_kmajor(st + a_bytes), dBl = tc::sdesc_kmajor(st + a_bytes + b_bytes);
                 bool neg = false;
                 if (MODE == MODE_CONTRACT) {
-                    unsigned long long k = (unsigned long long)(kb0 + kb) * MK;
-                    neg = (int)(k % (unsigned long long)a.nu_pad) >= a.npos_pad;
+                    neg = kmod >= a.npos_pad;
+                    kmod += MK;
+                    if (kmod >= a.nu_pad) kmod -= a.nu_pad;
                 }
+                const uint32_t i1 = neg ? id1n : id1p, i2 = neg ? id2n : id2p;
 #pragma unroll
                 for (int ks = 0; ks < MK / 16; ++ks) {
-                    const uint32_t koff = ks * 32;  // 16 bf16 along k
-#pragma unroll
-                    for (int p = 0; p < 3; ++p) {  // hi*hi, hi*lo, lo*hi
-                        uint32_t aa = (p == 2 ? aL : aH) + koff;
-                        uint32_t bb = (p == 1 ? bL : bH) + koff;
-                        for (int nc = 0; nc < N; nc += 256) {
-                            int nn = min(256, N - nc);
-                            uint32_t acc = (kb | ks | p) != 0 ? 1u : 0u;
-                            tc::mma_bf16(dcol + (uint32_t)nc, tc::sdesc_kmajor_sw64(aa),
-                                         tc::sdesc_kmajor_sw64(bb + (uint32_t)nc * MK * 2), tc::idesc_bf16_f32(MM, nn, neg),
-                                         acc);
-                        }
-                    }
+                    const uint64_t ko = (uint64_t)(2 * ks);  // 32 bytes along k, in 16-byte units
+                    const uint32_t acc0 = (kb | ks) != 0 ? 1u : 0u;
+                    // hi*hi, hi*lo, lo*hi
+                    tc::mma_bf16(d1, dAh + ko, dBh + ko, i1, acc0);
+                    if (n2 > 0) tc::mma_bf16(d2, dAh + ko, dBh + ko + boff2, i2, acc0);
+                    tc::mma_bf16(d1, dAh + ko, dBl + ko, i1, 1u);
+                    if (n2 > 0) tc::mma_bf16(d2, dAh + ko, dBl + ko + boff2, i2, 1u);
+                    tc::mma_bf16(d1, dAl + ko, dBh + ko, i1, 1u);
+                    if (n2 > 0) tc::mma_bf16(d2, dAl + ko, dBh + ko + boff2, i2, 1u);
                 }
                 tc::mma_commit(&empty[s]);
+                if (++s == a.stages) {
+                    s = 0;
+                    ph ^= 1u;
+                }
             }
             tc::mma_commit(&tfull[buf]);
             if (!ok) break;
@@ -266,7 +294,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
                     size_t k0 = Q * a.nu_pad + a.n_off + c0;
                     size_t blk = (rowblk + k0 / MK) * (size_t)(MM * MK);  // elements
                     uint32_t ch = (uint32_t)((k0 % MK) / 8);
-                    uint32_t o0 = tc::sw64_offset(rr, ch) / 2, o1 = tc::sw64_offset(rr, ch + 1) / 2;
+                    uint32_t o0 = tc::swz_offset(rr, ch) / 2, o1 = tc::swz_offset(rr, ch + 1) / 2;
                     *reinterpret_cast<uint4*>(a.Xhi + blk + o0) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
                     *reinterpret_cast<uint4*>(a.Xhi + blk + o1) = make_uint4(hi[4], hi[5], hi[6], hi[7]);
                     *reinterpret_cast<uint4*>(a.Xlo + blk + o0) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
@@ -322,7 +350,7 @@ __global__ void split_B_kernel(const double* __restrict__ B, int naux, int nbf, 
         __nv_bfloat16 h = __double2bfloat16(v);
         // pre-swizzled 8 KB blocks (128 rows x 32 k): the shared-memory image of an operand tile
         size_t blk = ((row / MM) * (size_t)(nbf_p / MK) + (size_t)(n / MK)) * (MM * MK);
-        size_t off = blk + tc::sw64_offset((uint32_t)(row % MM), (uint32_t)((n % MK) / 8)) / 2 + (n % 8);
+        size_t off = blk + tc::swz_offset((uint32_t)(row % MM), (uint32_t)((n % MK) / 8)) / 2 + (n % 8);
         Bh[off] = h;
         Bl[off] = __double2bfloat16(v - (double)__bfloat162float(h));
     }
@@ -343,9 +371,10 @@ __global__ void split_Ut_kernel(const double* __restrict__ U, int ldu, int nbf, 
         }
         double v = (col >= 0 && k < nbf) ? U[(size_t)k * ldu + col] : 0.0;
         __nv_bfloat16 h = __double2bfloat16(v);
-        // pre-swizzled 4 KB blocks (64 rows x 32 k)
-        size_t blk = ((size_t)(j / B_ROWS_PER_TMA) * (size_t)(nbf_p / MK) + (size_t)(k / MK)) * (B_ROWS_PER_TMA * MK);
-        size_t off = blk + tc::sw64_offset((uint32_t)(j % B_ROWS_PER_TMA), (uint32_t)((k % MK) / 8)) / 2 + (k % 8);
+        // k-block-major and pre-swizzled: all nu_pad rows of one 32-wide k block are contiguous,
+        // so a stage's whole U^T operand is one bulk copy
+        size_t off = (size_t)(k / MK) * ((size_t)nu_pad * MK) + tc::swz_offset((uint32_t)j, (uint32_t)((k % MK) / 8)) / 2 +
+                     (k % 8);
         Uh[off] = h;
         Ul[off] = __double2bfloat16(v - (double)__bfloat162float(h));
     }
@@ -491,8 +520,8 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         m->nbf_p = nbf_p;
         m->B_ready = true;
     }
-    const int npos_pad = round_up(npos, 64);
-    const int nneg_pad = round_up(nneg, 64);
+    const int npos_pad = round_up(npos, MK);
+    const int nneg_pad = round_up(nneg, MK);
     const int nu_pad = npos_pad + nneg_pad;
     if (nu_pad == 0) {
         cudaMemsetAsync(K, 0, sizeof(double) * (size_t)nbf * nbf, s);
@@ -538,16 +567,19 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         ta.Xlo = m->Xl;
         ta.err = m->err;
         ta.tiles = nullptr;
-        ta.zero_blk = nullptr;
+        ta.zero_blk = m->zero_blk;
         ta.Bsh = m->Bh;
         ta.Bsl = m->Bl;
         ta.Uth = m->Uh;
         ta.Utl = m->Ul;
+        // one 128-row tile per item; two TMEM accumulators when they fit, so the epilogue of one
+        // item overlaps the MMAs of the next
+        ta.n_mtiles = (int)((size_t)naux * nbf_p / MM);
         int stage_bytes = 2 * A_TILE_BYTES + 2 * ta.n_cols * MK * 2;
         ta.stages = std::min(8, (SMEM_BUDGET - SMEM_RESERVE) / stage_bytes);
         ta.nbuf = (2 * ta.n_cols <= 512) ? 2 : 1;
         ta.tmem_cols = pow2_cols(ta.nbuf * ta.n_cols);
-        ta.n_items = (int)((size_t)naux * nbf_p / MM);
+        ta.n_items = ta.n_mtiles;
         unsigned grid = (unsigned)std::min(ta.n_items, m->num_sms);
         tc_gemm_kernel<MODE_TRANSFORM><<<grid, TC_THREADS, SMEM_BUDGET, s>>>(ta);
     }

@@ -84,11 +84,17 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
-// Byte offset of (row r, 16-byte chunk c) inside a K-major operand tile with 64-byte rows and
-// the 64-byte swizzle (chunk index XOR bits 1-2 of the row): the layout TMA's
-// CU_TENSOR_MAP_SWIZZLE_64B writes and the sdesc_kmajor_sw64 descriptor reads.
-__host__ __device__ __forceinline__ uint32_t sw64_offset(uint32_t r, uint32_t c) {
-    return r * 64u + ((c ^ ((r >> 1) & 3u)) << 4);
+// Swizzle width of the K-major operand tiles (bytes per tile row): 64 or 128.
+#ifndef GDFJK_SWIZZLE_BYTES
+#define GDFJK_SWIZZLE_BYTES 64
+#endif
+constexpr uint32_t SWZ = GDFJK_SWIZZLE_BYTES;
+
+// Byte offset of (row r, 16-byte chunk c) inside a K-major operand tile with SWZ-byte rows and
+// the SWZ-byte swizzle (16-byte chunk index XOR address bits 7 and up): the layout TMA writes
+// with CU_TENSOR_MAP_SWIZZLE_64B / _128B and the sdesc_kmajor descriptor reads.
+__host__ __device__ __forceinline__ uint32_t swz_offset(uint32_t r, uint32_t c) {
+    return r * SWZ + ((c ^ (((r * SWZ) >> 7) & (SWZ / 16u - 1u))) << 4);
 }
 
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
@@ -108,16 +114,16 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
 // ---- descriptors
-// Shared-memory matrix descriptor, K-major operand with a 64-byte swizzle (rows of 32 bf16,
-// 8-row atoms of 512 bytes): start >> 4, LBO (unused for swizzled K-major) = 1, SBO = 512 B,
-// descriptor version 1, layout type SWIZZLE_64B.
-__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
+// Shared-memory matrix descriptor, K-major operand with an SWZ-byte swizzle (8-row atoms of
+// 8*SWZ bytes): start >> 4, LBO (unused for swizzled K-major) = 1, SBO = 8*SWZ bytes,
+// descriptor version 1, layout type SWIZZLE_64B (4) or SWIZZLE_128B (2).
+__device__ __forceinline__ uint64_t sdesc_kmajor(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFF);
     d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(512 >> 4) << 32;
+    d |= (uint64_t)((8 * SWZ) >> 4) << 32;
     d |= (uint64_t)1 << 46;
-    d |= (uint64_t)4 << 61;
+    d |= (uint64_t)(SWZ == 128 ? 2 : 4) << 61;
     return d;
 }
 
