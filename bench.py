@@ -307,6 +307,19 @@ def run_gpu(args):
         except Exception as ex:  # reported, not hidden
             out["mixed"] = {"unavailable": str(ex)[:300]}
 
+    if args.extra and rank == 0:
+        # other configurations (synthetic B of their shapes): FP64 build and the precision form
+        eng.close()
+        del C, J, K
+        torch.cuda.empty_cache()
+        out["extra_configs"] = {}
+        for cfg in [c for c in args.extra.split(",") if c]:
+            try:
+                out["extra_configs"][cfg] = measure_config(cfg, dev, args, peaks)
+            except Exception as ex:
+                out["extra_configs"][cfg] = {"unavailable": str(ex)[:300]}
+            torch.cuda.empty_cache()
+
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(nbf, naux, nocc, budget_s=args.cpu_budget)
     if rank == 0 and args.scf:
@@ -376,6 +389,54 @@ def measure_mixed(eng, C, J, K, nbf, naux, nocc, stream, args, peaks):
                                "note": "issued BF16 flops (3 split products, padded sizes) of measured burst bf16"},
         "scheme": "BF16x3: x = hi + lo (bf16), products hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM, FP64 split-K reduction",
     }
+
+
+def measure_config(cfg, dev, args, peaks):
+    """FP64 and precision-form builds/s for another configuration, synthetic B of its shape."""
+    import torch
+
+    from psi4_gb300 import _jkabi as abi
+    from psi4_gb300.jk import DFJKEngine
+
+    mol, nbf, naux, nocc, desc = workload_sizes(cfg)
+    npair = nbf * (nbf + 1) // 2
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4321)
+    eng = DFJKEngine(nbf, naux, None, device=dev.index or 0)
+    B = torch.empty((naux, npair), dtype=torch.float64, device=dev)
+    for q0 in range(0, naux, 256):
+        B[q0:min(naux, q0 + 256)].normal_(0.0, 0.02, generator=gen)
+    torch.cuda.synchronize()
+    eng.upload_device(B.data_ptr())
+    del B
+    torch.cuda.empty_cache()
+    C = torch.randn((nbf, nocc), dtype=torch.float64, device=dev, generator=gen) * 0.1
+    J = torch.empty((nbf, nbf), dtype=torch.float64, device=dev)
+    K = torch.empty_like(J)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+
+    def run(mode, n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            eng.compute_device(C.data_ptr(), None, nocc, nocc, mode, None, J.data_ptr(), K.data_ptr())
+        e1.record(stream)
+        eng.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / n
+
+    fp = abi.DO_J | abi.DO_K
+    run(fp, 1)
+    t64 = run(fp, 1)
+    tm64 = eng.timings()
+    out = {"workload": desc + " (synthetic B, dense)", "nbf": nbf, "naux": naux, "nocc": nocc,
+           "fp64": {"builds_per_s": 1.0 / t64, "ms_per_build": 1e3 * t64, "phase_ms": tm64}}
+    args._fp64_value = 1.0 / t64
+    out["mixed"] = measure_mixed(eng, C, J, K, nbf, naux, nocc, stream, args, peaks)
+    free, total = torch.cuda.mem_get_info(dev)
+    out["device_memory_in_use_gb"] = (total - free) / 1e9  # all engine buffers of both forms allocated
+    eng.close()
+    return out
 
 
 def measure_scf(cfg):
@@ -461,6 +522,7 @@ def main():
     ap.add_argument("--mixed", type=int, default=1)
     ap.add_argument("--scf", type=int, default=1)
     ap.add_argument("--scf-config", default="c4", choices=["c1", "c4"])
+    ap.add_argument("--extra", default="c3", help="comma-separated extra configurations (synthetic B), '' for none")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
