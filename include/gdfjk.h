@@ -50,7 +50,10 @@ enum {
     GDFJK_DO_K = 2,
     GDFJK_MIXED = 4,       /* K as a split-BF16 tensor-core product with FP32 accumulation      */
     GDFJK_INCREMENTAL = 8, /* K += K(dD) against the previous build's density (mixed form only)  */
-    GDFJK_RESET = 16       /* forget the incremental history (next build is a full build)      */
+    GDFJK_RESET = 16,      /* forget the incremental history (next build is a full build)      */
+    GDFJK_EMULATED = 32    /* K to FP64 accuracy from BF16 tensor-core products of 7-bit digit
+                              slices (Ozaki splitting, exact FP32 level sums, double-float
+                              epilogue); lr-symmetric densities; ignored with GDFJK_MIXED      */
 };
 
 /* Create an engine on CUDA device `device` for nbf basis functions and naux fitting

@@ -41,6 +41,7 @@ DO_K = 2
 MIXED = 4
 INCREMENTAL = 8
 RESET = 16
+EMULATED = 32
 
 NOALLOC_MAX_NAUX = 65536
 

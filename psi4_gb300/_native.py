@@ -25,7 +25,7 @@ INTS_SO = os.path.join(LIB, "libgdfints.so")
 JK_SO = os.path.join(LIB, "libgdfjk.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-JK_SOURCES = ["gdfjk_host.cu", "j_kernels.cu", "k_fp64.cu", "k_mixed.cu", "backward.cu", "noalloc.cu"]
+JK_SOURCES = ["gdfjk_host.cu", "j_kernels.cu", "k_fp64.cu", "k_mixed.cu", "k_oz.cu", "backward.cu", "noalloc.cu"]
 
 _lock = threading.Lock()
 

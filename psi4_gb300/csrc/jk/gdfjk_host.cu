@@ -22,6 +22,7 @@
 #include "gdfjk.h"
 #include "common.cuh"
 #include "mixed.cuh"
+#include "oz.cuh"
 
 using namespace gdfjk;
 
@@ -54,6 +55,7 @@ struct gdfjk_s {
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float t_j = 0, t_kt = 0, t_kc = 0;
     MixedState* mixed = nullptr;
+    OzState* oz = nullptr;
     // backward workspaces
     double *gJp = nullptr, *gKp = nullptr, *Jg = nullptr, *Yb = nullptr, *Zpart = nullptr, *dCp = nullptr;
     double *gq = nullptr, *Dw2 = nullptr, *Jgt = nullptr, *hC = nullptr, *hgJ = nullptr, *hgK = nullptr, *hdC = nullptr,
@@ -174,6 +176,21 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
             if (nonsym) return set_err(h, GDFJK_ERR_ARG, "mixed-precision K needs an lr-symmetric density");
             rc = mixed_build_K(h->mixed, h->B, L, h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
                                h->ev[3], s, h->err);
+            if (rc == GDFJK_ERR_OOM) {  // give the emulated form's caches back and retry once
+                CK(cudaStreamSynchronize(s));
+                oz_release(h->oz);
+                rc = mixed_build_K(h->mixed, h->B, L, h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
+                                   h->ev[3], s, h->err);
+            }
+            if (rc) return rc;
+        } else if (mode & GDFJK_EMULATED) {
+            if (nonsym) return set_err(h, GDFJK_ERR_ARG, "emulated-FP64 K needs an lr-symmetric density");
+            rc = oz_build_K(h->oz, h->B, L, h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
+            if (rc == GDFJK_ERR_OOM) {  // give the mixed form's split copy of B back and retry once
+                CK(cudaStreamSynchronize(s));
+                mixed_invalidate(h->mixed);
+                rc = oz_build_K(h->oz, h->B, L, h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
+            }
             if (rc) return rc;
         } else {
             launch_k_transform_fp64(h->B, h->Cl, h->naux, h->nbf_pad, nocc_pad, L, h->Xl, s);
@@ -216,6 +233,7 @@ int check_device_flag(gdfjk_t h) {
     CK(cudaMemcpyAsync(&flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     flag |= mixed_error_flag(h->mixed, h->stream);
+    flag |= oz_error_flag(h->oz, h->stream);
     if (flag) {
         CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
         if (flag & 4) return set_err(h, GDFJK_ERR_NUMERIC, "non-finite values in J or K");
@@ -249,6 +267,7 @@ int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes
     int ns = k_contract_splits((int)nbf_pad, (size_t)naux * std::max<size_t>(nocc_pad, 1), true);
     b += (size_t)ns * ntiles * TILE_ELEMS * 8;                   // split-K partials
     if (flags & GDFJK_MIXED) b += mixed_query_memory(nbf, naux, max_nocc);
+    if (flags & GDFJK_EMULATED) b += oz_query_memory(nbf, naux, max_nocc);
     *bytes = b;
     return GDFJK_OK;
 }
@@ -318,6 +337,7 @@ int gdfjk_create(int device, int nbf, int naux, const unsigned char* pair_mask, 
     cudaMemcpy(h->d_map, h->map.data(), sizeof(int) * h->map.size(), cudaMemcpyHostToDevice);
     cudaMemset(h->d_err, 0, sizeof(int));
     h->mixed = mixed_create();
+    h->oz = oz_create();
     if (cudaGetLastError() != cudaSuccess) {
         h->err = "create: CUDA error while initialising";
         return fail(GDFJK_ERR_CUDA);
@@ -340,6 +360,7 @@ int gdfjk_destroy(gdfjk_t h) {
     if (h->d_map) cudaFree(h->d_map);
     if (h->d_err) cudaFree(h->d_err);
     mixed_destroy(h->mixed);
+    oz_destroy(h->oz);
     for (auto& ev : h->ev)
         if (ev) cudaEventDestroy(ev);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -366,6 +387,7 @@ int gdfjk_upload_B_device(gdfjk_t h, const double* Bq) {
     CK(cudaGetLastError());
     if ((rc = wait_stream(h, env_timeout()))) return rc;
     mixed_invalidate(h->mixed);
+    oz_invalidate(h->oz);
     h->B_ready = true;
     return GDFJK_OK;
 }
@@ -447,6 +469,7 @@ int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_sk
     if (e != cudaSuccess) return set_err(h, GDFJK_ERR_CUDA, std::string("upload_B: ") + cudaGetErrorString(e));
     if (rc) return rc;
     mixed_invalidate(h->mixed);
+    oz_invalidate(h->oz);
     h->B_ready = true;
     return GDFJK_OK;
 }
@@ -532,8 +555,8 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
     }
     if ((mode & GDFJK_DO_K) && !(mode & GDFJK_MIXED)) {
         // FP64 anchor: a full FP64 K from C that becomes the base of later increments
-        rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_K, nullptr, nullptr,
-                           h->dK);
+        rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, nullptr, nocc, std::max(ldc, 1),
+                           GDFJK_DO_K | (mode & GDFJK_EMULATED), nullptr, nullptr, h->dK);
         if (rc) return rc;
         rc = mixed_set_base(h->mixed, h->dK, h->nbf, s, h->err);
         if (rc) return rc;

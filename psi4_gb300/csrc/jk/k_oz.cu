@@ -1,0 +1,1223 @@
+// k_oz.cu — FP64-accurate exchange on the BF16 tensor cores (digit-split, "Ozaki" scheme).
+//
+// K = sum_Q B_Q C C^T B_Q to FP64 accuracy, with every multiply-add on tcgen05 BF16 MMAs
+// (Ozaki, Ogita, Oishi & Rump 2012, "Error-free transformations of matrix multiplication by
+// using fast routines of matrix multiplication and its applications"; here with balanced
+// 7-bit digits so that BF16 holds each digit exactly).
+//
+// Digits.  A row (or row chunk) with |x| < 2^E is written in fixed point as
+//     v = round(x * 2^(47-E)),  |v| <= 2^47,   v = sum_{s=0..6} d_s 2^(7(6-s)),  d_s in [-64, 63]
+// so x = 2^(E-5) * sum_s g_s (+ |error| <= 2^(E-48)) with the slice values g_s = d_s 2^(-7s),
+// each exact in BF16.  The digits come from integer arithmetic on the IEEE bit pattern (no
+// FP64 instruction: this GPU's FP64 pipe runs at ~1/60 of its FP32 rate).
+//
+// Products.  (x y) = 2^(Ex+Ey-10) sum_{s+t<=6} g_s h_t  (28 slice pairs; the level-7 pairs
+// dropped and the digit remainders are ~2^-44 of |x|max|y|max per term).  Pairs are grouped
+// by level L = s+t into six tensor-memory accumulators: L = 0..4 each on its own, as sums of
+// integers times one power of two, exact in FP32 while a partial sum stays below 2^24 units
+// (provably for L <= 3 in a run of at most 1024 terms: 4 pairs x 1024 x 64^2 = 2^24; level 4
+// in all but adversarial digit patterns), and the tail L = 5, 6 prescaled.  The tensor cores'
+// FP32 accumulation rounds toward zero: on an inexact accumulator that holds positive terms
+// (the squares on the diagonal of K) the truncations add up to a bias, ~2^-36 relative with a
+// level-4 tail; with the tail at levels 5-6 it is 2^7 smaller.  The epilogue adds the six in
+// double-float (FP32 pairs).
+//
+//   half-transform   X[m][(Q,i)] = sum_n B_Q[m][n] C[n][i]      A = digits of B (int8 in HBM,
+//                    converted to BF16 slices in shared memory by four converter warps),
+//                    B = digits of C^T (BF16); one item = (Q, 128 rows, a chunk of <= 80
+//                    columns), k split into runs of <= 1024; X out in double-float plus a
+//                    row max per group of Q.
+//   split            X -> BF16 digit slices with one exponent per (row, group of Q), a group
+//                    being <= 1024 contraction terms.
+//   contraction      K[m][n] = sum_groups 2^(E_m+E_n-10) sum_pairs ... : 128 x 64 tiles of the
+//                    lower triangle; one accumulation run per group, drained into a
+//                    double-float running sum in registers; split over groups; FP64 partials
+//                    summed in a fixed order.
+// Each accumulation run covers its k range in three passes (A slices {0,1} with B slices
+// 0-6, {2,3} with 0-4, {4,5,6} with 0-2) so that one pipeline stage holds at most three
+// A slices and seven B slices.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gdfjk.h"
+#include "oz.cuh"
+#include "tc_common.cuh"
+
+namespace gdfjk {
+namespace oz {
+
+constexpr int MM = 128;                      // tile rows (MMA M)
+constexpr int MK = 32;                       // k per pipeline stage (one 64-byte row of BF16)
+constexpr int NSL = 7;                       // digit slices
+constexpr int NACC = 6;                      // accumulators: levels 0..4 and the tail (5, 6)
+constexpr int NPASS = 3;
+constexpr int I8_SLICE = MM * MK;            // bytes of one int8 digit slice of a 128 x 32 block
+constexpr int BF_SLICE = MM * MK * 2;        // bytes of one BF16 slice of a 128 x 32 block
+constexpr int I8_BLOCK = NSL * I8_SLICE;     // 28 KB: all slices of one 128 x 32 block of B
+constexpr int MAX_A_SLOTS = 3;               // A slices per pass, at most
+constexpr int E_EMPTY = -100000;             // exponent of an all-zero row
+constexpr int SMEM_BUDGET = 224 * 1024;
+constexpr int SMEM_RESERVE = 2048;
+constexpr int TR_THREADS = 320;              // producer, MMA, 4 epilogue warps, 4 converter warps
+constexpr int CT_THREADS = 192;              // producer, MMA, 4 epilogue warps
+constexpr int CT_N = 64;                     // contraction tile columns
+constexpr int TR_MAX_N = 80;                 // half-transform accumulator columns
+constexpr int RUN_K = 1024;                  // terms per exact accumulation run
+static_assert(tc::SWZ == 64, "digit slices are laid out for the 64-byte swizzle");
+
+// the three passes: first A slice, A slices, B slices
+__host__ __device__ __forceinline__ constexpr int pass_a0(int p) { return p == 0 ? 0 : (p == 1 ? 2 : 4); }
+__host__ __device__ __forceinline__ constexpr int pass_na(int p) { return p == 2 ? 3 : 2; }
+__host__ __device__ __forceinline__ constexpr int pass_nb(int p) { return p == 0 ? 7 : (p == 1 ? 5 : 3); }
+
+// offset added to v so that every base-128 digit field of u = v + OFF is d_s + 64 in [0, 127]
+constexpr unsigned long long DIGIT_OFF =
+    64ull * (1ull + (1ull << 7) + (1ull << 14) + (1ull << 21) + (1ull << 28) + (1ull << 35) + (1ull << 42));
+
+// E with |x| < 2^E for the largest magnitude |x| whose bits are given (sign cleared)
+__device__ __forceinline__ int exp_of_max_d(unsigned long long bits) {
+    if (bits == 0) return E_EMPTY;
+    int ex = (int)(bits >> 52);
+    if (ex == 0) ex = 1;
+    return ex - 1022;
+}
+__device__ __forceinline__ int exp_of_max_f(unsigned bits) {
+    if (bits == 0) return E_EMPTY;
+    int ex = (int)(bits >> 23);
+    if (ex == 0) ex = 1;
+    return ex - 126;
+}
+// 2^(E-5) as a float (the slice weight of a row); 0 for empty rows or below the normal range
+__device__ __forceinline__ float scale_of(int E) {
+    if (E == E_EMPTY) return 0.f;
+    int b = E - 5 + 127;
+    if (b <= 0) return 0.f;
+    if (b > 254) b = 254;
+    return __int_as_float(b << 23);
+}
+
+// round(x * 2^(47-E)) for |x| < 2^E, from the bit pattern
+__device__ __forceinline__ long long fix_d(double x, int E) {
+    if (E == E_EMPTY) return 0;
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    int ex = (int)((b >> 52) & 0x7FF);
+    unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    if (ex)
+        mant |= 1ull << 52;
+    else
+        ex = 1;
+    int r = 1028 + E - ex;  // >= 6 because |x| < 2^E
+    unsigned long long v = r >= 64 ? 0ull : ((mant + (1ull << (r - 1))) >> r);
+    return (b >> 63) ? -(long long)v : (long long)v;
+}
+__device__ __forceinline__ long long fix_f(float x, int E) {
+    if (E == E_EMPTY) return 0;
+    unsigned b = __float_as_uint(x);
+    int ex = (int)((b >> 23) & 255);
+    unsigned long long mant = b & 0x7FFFFFu;
+    if (ex)
+        mant |= 0x800000u;
+    else
+        ex = 1;
+    int sh = ex - 103 - E;  // <= 23 because |x| < 2^E
+    unsigned long long v;
+    if (sh >= 0) {
+        v = mant << sh;
+    } else {
+        int r = -sh;
+        v = r >= 40 ? 0ull : ((mant + (1ull << (r - 1))) >> r);
+    }
+    return (b >> 31) ? -(long long)v : (long long)v;
+}
+// digit field of slice s (0 = most significant) of u = v + DIGIT_OFF
+__device__ __forceinline__ uint32_t digit_field(unsigned long long u, int s) {
+    return (uint32_t)(u >> (7 * (NSL - 1 - s))) & 127u;
+}
+// BF16 bits of the slice value (f - 64) * 2^(-7s), exact; w = 2^(-7s)
+__device__ __forceinline__ uint32_t field_bf16(uint32_t f, float w) {
+    float g = fmaf(__uint_as_float(0x4B000000u | f), w, -8388672.0f * w);
+    return __float_as_uint(g) >> 16;
+}
+__device__ __forceinline__ float slice_weight(int s) { return __int_as_float((127 - 7 * s) << 23); }
+
+// ---------------------------------------------------------------- digits of B (once per upload)
+// Row maxima of |B_Q[m][.]| over both triangles from the stored tiles: rows of a stored tile
+// (I, J) belong to rows 64I+r, and for I != J its columns to rows 64J+c.
+__global__ void oz_rowmax_kernel(const double* __restrict__ B, int ntiles, const int* __restrict__ tI,
+                                 const int* __restrict__ tJ, int nbf_p, unsigned long long* __restrict__ rowmax) {
+    const size_t qt = blockIdx.x;  // Q * ntiles + t
+    const int Q = (int)(qt / ntiles), t = (int)(qt % ntiles);
+    const int I = tI[t], J = tJ[t];
+    const double* tile = B + qt * TILE_ELEMS;
+    __shared__ unsigned long long colpart[4][TILE];
+    {
+        // rows: 4 threads per row, 16 columns each
+        int r = threadIdx.x / 4, part = threadIdx.x % 4;
+        unsigned long long mx = 0;
+        for (int c = part * 16; c < part * 16 + 16; ++c) {
+            unsigned long long b = (unsigned long long)__double_as_longlong(tile[r * TILE + c]) & 0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+        if (part == 0 && mx) atomicMax(&rowmax[(size_t)Q * nbf_p + I * TILE + r], mx);
+    }
+    if (I != J) {
+        int c = threadIdx.x % TILE, part = threadIdx.x / TILE;
+        unsigned long long mx = 0;
+        for (int r = part * 16; r < part * 16 + 16; ++r) {
+            unsigned long long b = (unsigned long long)__double_as_longlong(tile[r * TILE + c]) & 0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+        colpart[part][c] = mx;
+        __syncthreads();
+        if (threadIdx.x < TILE) {
+            unsigned long long m2 = max(max(colpart[0][c], colpart[1][c]), max(colpart[2][c], colpart[3][c]));
+            if (m2) atomicMax(&rowmax[(size_t)Q * nbf_p + J * TILE + c], m2);
+        }
+    }
+}
+
+// Int8 digit fields of B, one 24 KB block per (Q, 128-row block, 32-wide k block):
+// [slice 6][row 128][k 32] of (d_s + 64).  Block (Q, mb, kb) = blockIdx.x; 256 threads.
+// The 128 x 32 FP64 window is staged in shared memory from the stored tiles (lower tiles
+// row-wise, upper ones through their stored mirror column-wise, both coalesced).
+__global__ void __launch_bounds__(256) oz_split_B_kernel(const double* __restrict__ B, int nbf, int nT, int ntiles,
+                                                         const int* __restrict__ map, int nbf_p,
+                                                         const unsigned long long* __restrict__ rowmax,
+                                                         float* __restrict__ sA, uint8_t* __restrict__ Bd) {
+    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
+    const size_t id = blockIdx.x;
+    const int kb = (int)(id % nkb);
+    const int mb = (int)((id / nkb) % nmb);
+    const int Q = (int)(id / ((size_t)nkb * nmb));
+    __shared__ double win[MM][MK + 1];
+    __shared__ int Es[MM];
+    const int J = (kb * MK) / TILE, c0 = (kb * MK) % TILE;
+    for (int h = 0; h < 2; ++h) {
+        const int I = mb * 2 + h;
+        int t = -1;
+        if (I < nT && J < nT) t = I >= J ? map[I * nT + J] : map[J * nT + I];
+        for (int e = threadIdx.x; e < TILE * MK; e += blockDim.x) {
+            double v = 0.0;
+            int r, c;
+            if (I >= J) {  // stored as rows r (of 64), columns c0 + c
+                r = e / MK;
+                c = e % MK;
+                if (t >= 0) v = B[((size_t)Q * ntiles + t) * TILE_ELEMS + r * TILE + c0 + c];
+            } else {  // stored mirror (J, I): element (m, n) at [n % 64][m % 64]
+                c = e / TILE;
+                r = e % TILE;
+                if (t >= 0) v = B[((size_t)Q * ntiles + t) * TILE_ELEMS + (c0 + c) * TILE + r];
+            }
+            const int m = I * TILE + r, n = J * TILE + c0 + c;
+            win[h * TILE + r][c] = (m < nbf && n < nbf) ? v : 0.0;
+        }
+    }
+    if (threadIdx.x < MM) {
+        const int m = mb * MM + threadIdx.x;
+        const int E = exp_of_max_d(rowmax[(size_t)Q * nbf_p + m]);
+        Es[threadIdx.x] = E;
+        if (kb == 0) sA[(size_t)Q * nbf_p + m] = scale_of(E);
+    }
+    __syncthreads();
+    uint8_t* out = Bd + id * I8_BLOCK;
+    for (int u = threadIdx.x; u < MM * (MK / 8); u += blockDim.x) {
+        const int r = u / (MK / 8), c8 = (u % (MK / 8)) * 8;
+        const int E = Es[r];
+        uint32_t w[NSL][2];
+#pragma unroll
+        for (int s = 0; s < NSL; ++s) w[s][0] = w[s][1] = 0u;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const unsigned long long uu = (unsigned long long)(fix_d(win[r][c8 + j], E) + (long long)DIGIT_OFF);
+#pragma unroll
+            for (int s = 0; s < NSL; ++s) w[s][j / 4] |= digit_field(uu, s) << (8 * (j % 4));
+        }
+#pragma unroll
+        for (int s = 0; s < NSL; ++s)
+            *reinterpret_cast<uint2*>(out + s * I8_SLICE + r * MK + c8) = make_uint2(w[s][0], w[s][1]);
+    }
+}
+
+// ---------------------------------------------------------------- digits of C (every build)
+// Column exponents of C (nbf x nocc_pad, row-major): one block per column slot i < ncols.
+__global__ void oz_col_scale_kernel(const double* __restrict__ C, int nbf, int nocc_pad, int nocc,
+                                    int* __restrict__ eC, float* __restrict__ sC) {
+    const int i = blockIdx.x;
+    unsigned long long mx = 0;
+    if (i < nocc)
+        for (int n = threadIdx.x; n < nbf; n += blockDim.x) {
+            unsigned long long b = (unsigned long long)__double_as_longlong(C[(size_t)n * nocc_pad + i]) &
+                                   0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+    __shared__ unsigned long long red[32];
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x / 32] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m2 = 0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) m2 = max(m2, red[w]);
+        const int E = exp_of_max_d(m2);
+        eC[i] = E;
+        sC[i] = scale_of(E);
+    }
+}
+
+// BF16 digit slices of C^T for the half-transform's B operand: [chunk][kb][slice][N rows][32 k],
+// each (N x 32) slice pre-swizzled (64-byte rows).  Thread = (column slot i, 8 consecutive n).
+__global__ void oz_split_C_kernel(const double* __restrict__ C, int nbf, int nbf_p, int nocc_pad, int N, int ncols,
+                                  const int* __restrict__ eC, __nv_bfloat16* __restrict__ Cd) {
+    const int n8 = nbf_p / 8;
+    const size_t total = (size_t)ncols * n8;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n8), n0 = (int)(e % n8) * 8;
+        const int E = eC[i];
+        uint32_t w[NSL][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = n0 + j;
+            const double x = (n < nbf && i < nocc_pad) ? C[(size_t)n * nocc_pad + i] : 0.0;
+            const unsigned long long uu = (unsigned long long)(fix_d(x, E) + (long long)DIGIT_OFF);
+#pragma unroll
+            for (int s = 0; s < NSL; ++s) {
+                const uint32_t bits = field_bf16(digit_field(uu, s), slice_weight(s));
+                if (j % 2 == 0)
+                    w[s][j / 2] = bits;
+                else
+                    w[s][j / 2] |= bits << 16;
+            }
+        }
+        const int chunk = i / N, row = i % N, kb = n0 / MK, c = (n0 % MK) / 8;
+        const int nkb = nbf_p / MK;
+        __nv_bfloat16* base = Cd + ((size_t)chunk * nkb + kb) * NSL * N * MK;
+        const uint32_t off = tc::swz_offset((uint32_t)row, (uint32_t)c) / 2;
+#pragma unroll
+        for (int s = 0; s < NSL; ++s)
+            *reinterpret_cast<uint4*>(base + (size_t)s * N * MK + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    }
+}
+
+// ---------------------------------------------------------------- shared pieces of the GEMMs
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// a[0] + ... + a[5] as an unevaluated FP32 pair (hi, lo): a[0..4] are the exact level sums,
+// a[5] the small tail; TwoSums and a final Fast2Sum keep the error near 2^-45 |hi|.
+__device__ __forceinline__ void combine6(const float* a, float& hi, float& lo) {
+    float s, e1, e2, e3, e4;
+    two_sum(a[0], a[1], s, e1);
+    two_sum(s, a[2], s, e2);
+    two_sum(s, a[3], s, e3);
+    two_sum(s, a[4], s, e4);
+    const float l = __fadd_rn(__fadd_rn(__fadd_rn(e1, e2), __fadd_rn(e3, e4)), a[5]);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
+}
+
+// (H, L) += (hi, lo), double-float
+__device__ __forceinline__ void df_add(float& H, float& L, float hi, float lo) {
+    float s, e;
+    two_sum(H, hi, s, e);
+    const float l = __fadd_rn(L, __fadd_rn(e, lo));
+    H = __fadd_rn(s, l);
+    L = __fsub_rn(l, __fsub_rn(H, s));
+}
+
+// The slice pairs of one 16-deep k step of pass `pass` (A slot j = slice pass_a0 + j, B slot
+// t = slice t).  d[L] accumulates level L = 0..4, d[5] the tail (levels 5, 6); `f` = 0 starts
+// a fresh accumulation run (every accumulator is first written in pass 0).
+__device__ __forceinline__ void issue_pairs(int pass, const uint32_t* d, uint64_t a0, uint64_t b0, uint64_t a_step,
+                                            uint64_t b_step, uint32_t id, uint32_t f) {
+    const uint64_t a1 = a0 + a_step, a2 = a0 + 2 * a_step;
+    const uint64_t b1 = b0 + b_step, b2 = b0 + 2 * b_step, b3 = b0 + 3 * b_step, b4 = b0 + 4 * b_step;
+    if (pass == 0) {  // slices 0, 1 x 0..6
+        const uint64_t b5 = b0 + 5 * b_step, b6 = b0 + 6 * b_step;
+        tc::mma_bf16(d[0], a0, b0, id, f);
+        tc::mma_bf16(d[1], a0, b1, id, f);
+        tc::mma_bf16(d[1], a1, b0, id, 1u);
+        tc::mma_bf16(d[2], a0, b2, id, f);
+        tc::mma_bf16(d[2], a1, b1, id, 1u);
+        tc::mma_bf16(d[3], a0, b3, id, f);
+        tc::mma_bf16(d[3], a1, b2, id, 1u);
+        tc::mma_bf16(d[4], a0, b4, id, f);
+        tc::mma_bf16(d[4], a1, b3, id, 1u);
+        tc::mma_bf16(d[5], a0, b5, id, f);
+        tc::mma_bf16(d[5], a1, b4, id, 1u);
+        tc::mma_bf16(d[5], a0, b6, id, 1u);
+        tc::mma_bf16(d[5], a1, b5, id, 1u);
+    } else if (pass == 1) {  // slices 2, 3 x 0..4
+        tc::mma_bf16(d[2], a0, b0, id, 1u);
+        tc::mma_bf16(d[3], a0, b1, id, 1u);
+        tc::mma_bf16(d[3], a1, b0, id, 1u);
+        tc::mma_bf16(d[4], a0, b2, id, 1u);
+        tc::mma_bf16(d[4], a1, b1, id, 1u);
+        tc::mma_bf16(d[5], a0, b3, id, 1u);
+        tc::mma_bf16(d[5], a1, b2, id, 1u);
+        tc::mma_bf16(d[5], a0, b4, id, 1u);
+        tc::mma_bf16(d[5], a1, b3, id, 1u);
+    } else {  // slices 4, 5, 6 x 0..2
+        tc::mma_bf16(d[4], a0, b0, id, 1u);
+        tc::mma_bf16(d[5], a0, b1, id, 1u);
+        tc::mma_bf16(d[5], a1, b0, id, 1u);
+        tc::mma_bf16(d[5], a0, b2, id, 1u);
+        tc::mma_bf16(d[5], a1, b1, id, 1u);
+        tc::mma_bf16(d[5], a2, b0, id, 1u);
+    }
+}
+
+// ---------------------------------------------------------------- half-transform
+struct TrArgs {
+    const uint8_t* Bd;         // int8 digit fields of B, [Q][mb][kb][7][128][32]
+    const __nv_bfloat16* Cd;   // BF16 digit slices of C^T, [chunk][kb][7][N][32]
+    const float* sA;           // [Q][nbf_p] slice weight 2^(E-5) of each row of B
+    const float* sC;           // [nchunk * N] slice weight of each column of C
+    float2* Xdf;               // [nbf][kdim_b] X as (hi, lo), k = (Q - q0) * nocc_p + i
+    unsigned* xmax;            // [nbf][ngroups] max |hi| per (row, group of G aux functions)
+    int q0, nq, nmb, nkb, nbf, nbf_p, nocc_p, N, nchunk, G, ngroups;
+    int run_kb, nrun;          // k blocks per accumulation run, runs per item
+    size_t kdim_b;
+    int stages, nbuf, tmem_cols, n_items;
+    int* err;
+};
+
+constexpr int TR_OFF_I8 = 0;                                  // <= 3 int8 slices of A (12 KB)
+constexpr int TR_OFF_BF = MAX_A_SLOTS * I8_SLICE;             // <= 3 BF16 slices of A (24 KB)
+constexpr int TR_OFF_C = TR_OFF_BF + MAX_A_SLOTS * BF_SLICE;  // <= 7 BF16 slices of C^T (N rows)
+
+__device__ __forceinline__ void tr_item(const TrArgs& a, int item, int& Q, int& mb, int& chunk) {
+    chunk = item % a.nchunk;
+    const int rest = item / a.nchunk;
+    mb = rest % a.nmb;
+    Q = a.q0 + rest / a.nmb;
+}
+__device__ __forceinline__ void tr_run(const TrArgs& a, int run, int& kb0, int& kb1) {
+    kb0 = run * a.run_kb;
+    kb1 = min(a.nkb, kb0 + a.run_kb);
+}
+
+// Persistent, warp-specialised: warp 0 lane 0 bulk-copies int8 A and BF16 C^T slices into a
+// ring of stages; warps 6-9 convert the int8 digit fields to BF16 slice values in the stage;
+// warp 1 lane 0 issues the slice-pair MMAs into six accumulators; warps 2-5 drain them
+// (tcgen05.ld) after every run into double-float X, and take the per-group row maxima.
+__global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int N = a.N;
+    const int c_slice = N * MK * 2;
+    const int stage_bytes = TR_OFF_C + NSL * c_slice;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * stage_bytes);
+    uint64_t* conv = full + a.stages;
+    uint64_t* empty = conv + a.stages;
+    uint64_t* tfull = empty + a.stages;  // [2]
+    uint64_t* tempty = tfull + 2;        // [2]
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+    const int warp = threadIdx.x / 32;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < a.stages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&conv[s], 128);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 4);
+        }
+        *abort_flag = 0;
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) tc::tmem_alloc(tmem_holder, (uint32_t)a.tmem_cols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    if (threadIdx.x == 0) {
+        // ---- producer
+        int s = 0;
+        uint32_t ph = 0;
+        long kg = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
+            int Q, mb, chunk;
+            tr_item(a, item, Q, mb, chunk);
+            const uint8_t* pa = a.Bd + ((size_t)Q * a.nmb + mb) * a.nkb * I8_BLOCK;
+            const __nv_bfloat16* pc = a.Cd + (size_t)chunk * a.nkb * NSL * N * MK;
+            for (int run = 0; ok && run < a.nrun; ++run) {
+                int kb0, kb1;
+                tr_run(a, run, kb0, kb1);
+                for (int pass = 0; ok && pass < NPASS; ++pass) {
+                    const uint32_t ab = (uint32_t)(pass_na(pass) * I8_SLICE);
+                    const uint32_t cb = (uint32_t)(pass_nb(pass) * c_slice);
+                    for (int kb = kb0; kb < kb1; ++kb, ++kg) {
+                        if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        uint8_t* st = smem + (size_t)s * stage_bytes;
+                        tc::mbar_arrive_expect_tx(&full[s], ab + cb);
+                        tc::bulk_load(st + TR_OFF_I8, pa + (size_t)kb * I8_BLOCK + pass_a0(pass) * I8_SLICE, ab, &full[s]);
+                        tc::bulk_load(st + TR_OFF_C, pc + (size_t)kb * NSL * N * MK, cb, &full[s]);
+                        if (++s == a.stages) {
+                            s = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+            }
+        }
+    } else if (warp >= 6) {
+        // ---- converters: int8 fields (d + 64) -> BF16 (d * 2^(-7 slice)), swizzled K-major
+        const int ct = threadIdx.x - 192;
+        int s = 0;
+        uint32_t ph = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
+            for (int run = 0; ok && run < a.nrun; ++run) {
+                int kb0, kb1;
+                tr_run(a, run, kb0, kb1);
+                for (int pass = 0; ok && pass < NPASS; ++pass) {
+                    const int units = pass_na(pass) * MM * (MK / 8);
+                    for (int kb = kb0; kb < kb1; ++kb) {
+                        if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        uint8_t* st = smem + (size_t)s * stage_bytes;
+                        for (int u = ct; u < units; u += 128) {
+                            const int j = u / (MM * (MK / 8));
+                            const int rem = u % (MM * (MK / 8));
+                            const int r = rem / (MK / 8), c = rem % (MK / 8);
+                            const uint2 q = *reinterpret_cast<const uint2*>(st + TR_OFF_I8 + j * I8_SLICE + r * MK + c * 8);
+                            const float w = slice_weight(pass_a0(pass) + j);
+                            const float off = -8388672.0f * w;
+                            uint32_t o[4];
+#pragma unroll
+                            for (int h = 0; h < 4; ++h) {
+                                const uint32_t word = h < 2 ? q.x : q.y;
+                                const uint32_t b0 = __byte_perm(word, 0x4B000000u, 0x7440u | (uint32_t)((2 * h) % 4));
+                                const uint32_t b1 = __byte_perm(word, 0x4B000000u, 0x7440u | (uint32_t)((2 * h + 1) % 4));
+                                const float g0 = fmaf(__uint_as_float(b0), w, off);
+                                const float g1 = fmaf(__uint_as_float(b1), w, off);
+                                o[h] = __byte_perm(__float_as_uint(g0), __float_as_uint(g1), 0x7632u);
+                            }
+                            *reinterpret_cast<uint4*>(st + TR_OFF_BF + j * BF_SLICE +
+                                                      tc::swz_offset((uint32_t)r, (uint32_t)c)) = make_uint4(o[0], o[1], o[2], o[3]);
+                        }
+                        fence_proxy_async();
+                        tc::mbar_arrive(&conv[s]);
+                        if (++s == a.stages) {
+                            s = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+            }
+        }
+    } else if (threadIdx.x == 32) {
+        // ---- MMA issuer
+        int s = 0;
+        uint32_t ph = 0;
+        int ri = 0;  // accumulation runs issued by this CTA
+        const uint32_t smem_base = tc::smem_u32(smem);
+        const uint32_t id = tc::idesc_bf16_f32(MM, N, false);
+        const uint64_t a_step = (uint64_t)(BF_SLICE >> 4), b_step = (uint64_t)(c_slice >> 4);
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
+            for (int run = 0; ok && run < a.nrun; ++run, ++ri) {
+                const int buf = ri % a.nbuf, use = ri / a.nbuf;
+                if (use > 0 && !tc::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), abort_flag, a.err)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t d0 = tmem + (uint32_t)(buf * NACC * N);
+                uint32_t d[NACC];
+#pragma unroll
+                for (int L = 0; L < NACC; ++L) d[L] = d0 + (uint32_t)(L * N);
+                int kb0, kb1;
+                tr_run(a, run, kb0, kb1);
+                for (int pass = 0; ok && pass < NPASS; ++pass) {
+                    for (int kb = kb0; kb < kb1; ++kb) {
+                        if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err) ||
+                            !tc::mbar_wait(&conv[s], ph, abort_flag, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint32_t st = smem_base + (uint32_t)(s * stage_bytes);
+                        const uint64_t dA = tc::sdesc_kmajor(st + TR_OFF_BF), dB = tc::sdesc_kmajor(st + TR_OFF_C);
+#pragma unroll
+                        for (int ks = 0; ks < MK / 16; ++ks) {
+                            const uint64_t ko = (uint64_t)(2 * ks);
+                            issue_pairs(pass, d, dA + ko, dB + ko, a_step, b_step, id, (pass | (kb - kb0) | ks) != 0 ? 1u : 0u);
+                        }
+                        tc::mma_commit(&empty[s]);
+                        if (++s == a.stages) {
+                            s = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+                tc::mma_commit(&tfull[buf]);
+            }
+        }
+    } else if (warp >= 2) {
+        // ---- epilogue: after each run, X (+)= run sum; after the last, the row maximum
+        const int q = warp % 4;
+        const int r = q * 32 + (threadIdx.x % 32);
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        int ri = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
+            int Q, mb, chunk;
+            tr_item(a, item, Q, mb, chunk);
+            const int m = mb * MM + r;
+            const bool valid = m < a.nbf;
+            const float sa = valid ? a.sA[(size_t)Q * a.nbf_p + m] : 0.f;
+            float2* xrow = a.Xdf + (valid ? (size_t)m * a.kdim_b + (size_t)(Q - a.q0) * a.nocc_p : 0);
+            float rmax = 0.f;
+            for (int run = 0; run < a.nrun; ++run, ++ri) {
+                const int buf = ri % a.nbuf, use = ri / a.nbuf;
+                ok = tc::mbar_wait(&tfull[buf], (uint32_t)(use & 1), abort_flag, a.err);
+                __syncwarp();
+                if (!ok || *abort_flag) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t cb = lane_base + (uint32_t)(buf * NACC * N);
+                const bool last = run == a.nrun - 1;
+                for (int c0 = 0; c0 < N; c0 += 8) {
+                    uint32_t v[NACC][8];
+#pragma unroll
+                    for (int L = 0; L < NACC; ++L) tc::tmem_ld8(cb + (uint32_t)(L * N + c0), v[L]);
+                    const int i0 = chunk * N + c0;
+                    if (valid) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int i = i0 + j;
+                            if (i < a.nocc_p) {
+                                float acc[NACC];
+#pragma unroll
+                                for (int L = 0; L < NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
+                                float hi, lo;
+                                combine6(acc, hi, lo);
+                                const float sc = sa * a.sC[i];
+                                hi *= sc;
+                                lo *= sc;
+                                if (run > 0) {
+                                    const float2 prev = xrow[i];
+                                    float H = prev.x, Lo = prev.y;
+                                    df_add(H, Lo, hi, lo);
+                                    hi = H;
+                                    lo = Lo;
+                                }
+                                xrow[i] = make_float2(hi, lo);
+                                if (last) rmax = fmaxf(rmax, fabsf(hi));
+                            }
+                        }
+                    }
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[buf]);
+            }
+            if (ok && valid && rmax > 0.f)
+                atomicMax(&a.xmax[(size_t)m * a.ngroups + (Q - a.q0) / a.G], __float_as_uint(rmax));
+        }
+    }
+    __syncwarp();
+    if (*abort_flag && threadIdx.x == 0) {
+        // let copies already issued land before the block's shared memory goes away
+        uint64_t t0 = tc::global_timer();
+        while (tc::global_timer() - t0 < 10000000ull) {
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+}
+
+// ---------------------------------------------------------------- split of X
+// X (double-float) -> BF16 digit slices for the contraction, [mb][kbt][7][128][32] pre-swizzled,
+// one exponent per (row, group); also the slice weights Sx[g][m] = 2^(E-5).
+// Block = (128-row block, group); 256 threads, thread unit = (row, 8 consecutive k).
+__global__ void __launch_bounds__(256) oz_split_X_kernel(const float2* __restrict__ Xdf, const unsigned* __restrict__ xmax,
+                                                         int nbf, int nbf_p, int ngroups, int G, int nq, int nocc_p,
+                                                         size_t kdim_b, size_t nkbt, float* __restrict__ Sx,
+                                                         __nv_bfloat16* __restrict__ Xd) {
+    const int mb = blockIdx.x, g = blockIdx.y;
+    __shared__ int Es[MM];
+    if (threadIdx.x < MM) {
+        const int m = mb * MM + threadIdx.x;
+        const int E = m < nbf ? exp_of_max_f(xmax[(size_t)m * ngroups + g]) : E_EMPTY;
+        Es[threadIdx.x] = E;
+        Sx[(size_t)g * nbf_p + m] = scale_of(E);
+    }
+    __syncthreads();
+    const int kb0 = g * G * nocc_p / MK;
+    const int kb1 = min(nq, (g + 1) * G) * nocc_p / MK;
+    const int units = (kb1 - kb0) * MM * (MK / 8);
+    for (int u = threadIdx.x; u < units; u += blockDim.x) {
+        const int kb = kb0 + u / (MM * (MK / 8));
+        const int rem = u % (MM * (MK / 8));
+        const int r = rem / (MK / 8), c = rem % (MK / 8);
+        const int m = mb * MM + r;
+        const int E = Es[r];
+        uint32_t w[NSL][4];
+#pragma unroll
+        for (int s = 0; s < NSL; ++s) w[s][0] = w[s][1] = w[s][2] = w[s][3] = 0u;
+        if (E != E_EMPTY) {
+            const float4* src = reinterpret_cast<const float4*>(Xdf + (size_t)m * kdim_b + (size_t)kb * MK + c * 8);
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const float4 x = src[p];  // two (hi, lo) pairs
+                const unsigned long long u0 = (unsigned long long)(fix_f(x.x, E) + fix_f(x.y, E) + (long long)DIGIT_OFF);
+                const unsigned long long u1 = (unsigned long long)(fix_f(x.z, E) + fix_f(x.w, E) + (long long)DIGIT_OFF);
+#pragma unroll
+                for (int s = 0; s < NSL; ++s) {
+                    const float wt = slice_weight(s);
+                    w[s][p] = field_bf16(digit_field(u0, s), wt) | (field_bf16(digit_field(u1, s), wt) << 16);
+                }
+            }
+        }
+        __nv_bfloat16* base = Xd + ((size_t)mb * nkbt + kb) * NSL * (MM * MK);
+        const uint32_t off = tc::swz_offset((uint32_t)r, (uint32_t)c) / 2;
+#pragma unroll
+        for (int s = 0; s < NSL; ++s)
+            *reinterpret_cast<uint4*>(base + (size_t)s * (MM * MK) + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    }
+}
+
+// ---------------------------------------------------------------- contraction
+struct CtArgs {
+    const __nv_bfloat16* Xd;  // [mb][kbt][7][128][32]
+    const float* Sx;          // [group][nbf_p]
+    const int2* tiles;        // (128-row block, 64-row block) of the lower triangle
+    int ntiles, nsplit, gps, ngroups, G, nocc_p, nq, nbf_p;
+    size_t nkbt;
+    double* part;  // [nsplit][ntiles][128][64]
+    int stages, nbuf, n_items;
+    int* err;
+};
+
+constexpr int CT_OFF_B = MAX_A_SLOTS * BF_SLICE;          // A: <= 3 slices of 128 rows (24 KB)
+constexpr int CT_STAGE = CT_OFF_B + NSL * CT_N * MK * 2;  // B: <= 7 slices of 64 rows (28 KB)
+
+__device__ __forceinline__ void ct_item(const CtArgs& a, int item, int& tile, int& g0, int& g1) {
+    const int split = item / a.ntiles;  // split-major: concurrent CTAs share one k window in L2
+    tile = item % a.ntiles;
+    g0 = split * a.gps;
+    g1 = min(a.ngroups, g0 + a.gps);
+}
+__device__ __forceinline__ int ct_kb0(const CtArgs& a, int g) { return g * a.G * a.nocc_p / MK; }
+__device__ __forceinline__ int ct_kb1(const CtArgs& a, int g) { return min(a.nq, (g + 1) * a.G) * a.nocc_p / MK; }
+
+__global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * CT_STAGE);
+    uint64_t* empty = full + a.stages;
+    uint64_t* tfull = empty + a.stages;  // [2]
+    uint64_t* tempty = tfull + 2;        // [2]
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+    const int warp = threadIdx.x / 32;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < a.stages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 4);
+        }
+        *abort_flag = 0;
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) tc::tmem_alloc(tmem_holder, 512u);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+    const size_t blk = (size_t)MM * MK;  // elements of one slice block
+
+    if (threadIdx.x == 0) {
+        // ---- producer
+        int s = 0;
+        uint32_t ph = 0;
+        long kg = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
+            int tile, g0, g1;
+            ct_item(a, item, tile, g0, g1);
+            const int2 tb = a.tiles[tile];
+            const __nv_bfloat16* pa = a.Xd + (size_t)tb.x * a.nkbt * NSL * blk;
+            const __nv_bfloat16* pb = a.Xd + (size_t)(tb.y / 2) * a.nkbt * NSL * blk + (size_t)(tb.y % 2) * (CT_N * MK);
+            for (int g = g0; ok && g < g1; ++g) {
+                const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
+                for (int pass = 0; ok && pass < NPASS; ++pass) {
+                    const int na = pass_na(pass), nb = pass_nb(pass);
+                    for (int kb = kb0; kb < kb1; ++kb, ++kg) {
+                        if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        uint8_t* st = smem + (size_t)s * CT_STAGE;
+                        tc::mbar_arrive_expect_tx(&full[s], (uint32_t)(na * BF_SLICE + nb * CT_N * MK * 2));
+                        tc::bulk_load(st, pa + ((size_t)kb * NSL + pass_a0(pass)) * blk, (uint32_t)(na * BF_SLICE), &full[s]);
+                        for (int t = 0; t < nb; ++t)
+                            tc::bulk_load(st + CT_OFF_B + t * (CT_N * MK * 2), pb + ((size_t)kb * NSL + t) * blk,
+                                          CT_N * MK * 2, &full[s]);
+                        if (++s == a.stages) {
+                            s = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+            }
+        }
+    } else if (threadIdx.x == 32) {
+        // ---- MMA issuer: one accumulation run (three passes) per group
+        int s = 0;
+        uint32_t ph = 0;
+        int gi = 0;
+        const uint32_t smem_base = tc::smem_u32(smem);
+        const uint32_t id = tc::idesc_bf16_f32(MM, CT_N, false);
+        const uint64_t a_step = (uint64_t)(BF_SLICE >> 4), b_step = (uint64_t)((CT_N * MK * 2) >> 4);
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
+            int tile, g0, g1;
+            ct_item(a, item, tile, g0, g1);
+            for (int g = g0; ok && g < g1; ++g, ++gi) {
+                const int buf = gi % a.nbuf, use = gi / a.nbuf;
+                if (use > 0 && !tc::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), abort_flag, a.err)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t d0 = tmem + (uint32_t)(buf * NACC * CT_N);
+                uint32_t d[NACC];
+#pragma unroll
+                for (int L = 0; L < NACC; ++L) d[L] = d0 + (uint32_t)(L * CT_N);
+                const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
+                for (int pass = 0; ok && pass < NPASS; ++pass) {
+                    for (int kb = kb0; kb < kb1; ++kb) {
+                        if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint32_t st = smem_base + (uint32_t)(s * CT_STAGE);
+                        const uint64_t dA = tc::sdesc_kmajor(st), dB = tc::sdesc_kmajor(st + CT_OFF_B);
+#pragma unroll
+                        for (int ks = 0; ks < MK / 16; ++ks) {
+                            const uint64_t ko = (uint64_t)(2 * ks);
+                            issue_pairs(pass, d, dA + ko, dB + ko, a_step, b_step, id,
+                                        (pass | (kb - kb0) | ks) != 0 ? 1u : 0u);
+                        }
+                        tc::mma_commit(&empty[s]);
+                        if (++s == a.stages) {
+                            s = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+                tc::mma_commit(&tfull[buf]);
+            }
+        }
+    } else if (warp >= 2) {
+        // ---- epilogue: per group, scale the six accumulators and add them into a
+        // double-float running sum (64 columns per thread); one FP64 partial tile per item
+        const int q = warp % 4;
+        const int r = q * 32 + (threadIdx.x % 32);
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        int gi = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
+            int tile, g0, g1;
+            ct_item(a, item, tile, g0, g1);
+            const int2 tb = a.tiles[tile];
+            const int m = tb.x * MM + r;
+            const int n0 = tb.y * CT_N;
+            float RH[CT_N], RL[CT_N];
+#pragma unroll
+            for (int c = 0; c < CT_N; ++c) RH[c] = RL[c] = 0.f;
+            for (int g = g0; g < g1; ++g, ++gi) {
+                const int buf = gi % a.nbuf, use = gi / a.nbuf;
+                ok = tc::mbar_wait(&tfull[buf], (uint32_t)(use & 1), abort_flag, a.err);
+                __syncwarp();
+                if (!ok || *abort_flag) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const float rs = a.Sx[(size_t)g * a.nbf_p + m];
+                const float* cs = a.Sx + (size_t)g * a.nbf_p + n0;
+                const uint32_t cb = lane_base + (uint32_t)(buf * NACC * CT_N);
+#pragma unroll
+                for (int c0 = 0; c0 < CT_N; c0 += 8) {
+                    uint32_t v[NACC][8];
+#pragma unroll
+                    for (int L = 0; L < NACC; ++L) tc::tmem_ld8(cb + (uint32_t)(L * CT_N + c0), v[L]);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        float acc[NACC];
+#pragma unroll
+                        for (int L = 0; L < NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
+                        float hi, lo;
+                        combine6(acc, hi, lo);
+                        const float sc = rs * cs[c0 + j];
+                        df_add(RH[c0 + j], RL[c0 + j], hi * sc, lo * sc);
+                    }
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[buf]);
+            }
+            if (!ok) break;
+            double* dst = a.part + (((size_t)(item / a.ntiles) * a.ntiles + tile) * MM + r) * CT_N;
+#pragma unroll
+            for (int c = 0; c < CT_N; c += 2)
+                *reinterpret_cast<double2*>(dst + c) =
+                    make_double2((double)RH[c] + (double)RL[c], (double)RH[c + 1] + (double)RL[c + 1]);
+        }
+    }
+    __syncwarp();
+    if (*abort_flag && threadIdx.x == 0) {
+        uint64_t t0 = tc::global_timer();
+        while (tc::global_timer() - t0 < 10000000ull) {
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 512u);
+}
+
+// K[m][n] (and its mirror), m >= n, = [K +] sum over splits (fixed order) of the partial tiles.
+__global__ void oz_reduce_kernel(const double* __restrict__ part, int nsplit, int ntiles, int nbf,
+                                 const int* __restrict__ tob, int ncb, double* __restrict__ K, int accumulate) {
+    const size_t n_lower = (size_t)nbf * (nbf + 1) / 2;
+    const size_t tstride = (size_t)ntiles * MM * CT_N;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n_lower; p += (size_t)gridDim.x * blockDim.x) {
+        size_t m = (size_t)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+        while (m * (m + 1) / 2 > p) --m;
+        while ((m + 1) * (m + 2) / 2 <= p) ++m;
+        const size_t n = p - m * (m + 1) / 2;
+        const int t = tob[(m / MM) * ncb + n / CT_N];
+        const size_t off = ((size_t)t * MM + (m % MM)) * CT_N + (n % CT_N);
+        double s = 0.0;
+        for (int k = 0; k < nsplit; ++k) s += part[(size_t)k * tstride + off];
+        if (accumulate) s += K[m * nbf + n];
+        K[m * nbf + n] = s;
+        K[n * nbf + m] = s;
+    }
+}
+
+}  // namespace oz
+
+// ---------------------------------------------------------------- host side
+struct OzState {
+    int nbf_p = 0;
+    uint8_t* Bd = nullptr;                 // int8 digit fields of B
+    float* sA = nullptr;                   // row weights of B
+    unsigned long long* rowmax = nullptr;  // row maxima of |B| (bits)
+    bool B_ready = false;
+    int* eC = nullptr;
+    float* sC = nullptr;
+    __nv_bfloat16* Cd = nullptr;
+    size_t C_cap = 0, sc_cap = 0;
+    float2* Xdf = nullptr;
+    __nv_bfloat16* Xd = nullptr;
+    size_t X_cap = 0;  // aux functions per batch the X buffers hold
+    unsigned* xmax = nullptr;
+    float* Sx = nullptr;
+    size_t xm_cap = 0, sx_cap = 0;
+    double* part = nullptr;
+    size_t part_cap = 0;
+    int2* d_tiles = nullptr;
+    int* d_tob = nullptr;
+    int tiles_nbf_p = 0, ntiles = 0, ncb = 0;
+    int* err = nullptr;
+    int num_sms = 0;
+    bool attrs_set = false;
+};
+
+OzState* oz_create() { return new OzState(); }
+
+namespace {
+
+int oz_alloc(void** p, size_t bytes, std::string& err) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        err = "emulated FP64: device allocation of " + std::to_string(bytes / 1e9) + " GB refused";
+        return GDFJK_ERR_OOM;
+    }
+    return GDFJK_OK;
+}
+
+void oz_free(void** p) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+}
+
+int pow2_cols(int n) {
+    int c = 32;
+    while (c < n) c <<= 1;
+    return c;
+}
+
+double x_cap_bytes() {
+    const char* s = getenv("GDFJK_OZ_XCAP_GB");
+    double gb = s ? atof(s) : 24.0;
+    if (!(gb > 0.0)) gb = 24.0;
+    return gb * 1e9;
+}
+
+}  // namespace
+
+void oz_release(OzState* o) {
+    if (!o) return;
+    oz_free((void**)&o->Bd);
+    oz_free((void**)&o->sA);
+    oz_free((void**)&o->rowmax);
+    oz_free((void**)&o->Xdf);
+    oz_free((void**)&o->Xd);
+    o->X_cap = 0;
+    o->B_ready = false;
+}
+
+void oz_invalidate(OzState* o) {
+    if (!o) return;
+    oz_free((void**)&o->Bd);
+    o->B_ready = false;
+}
+
+void oz_destroy(OzState* o) {
+    if (!o) return;
+    oz_release(o);
+    void* ps[] = {o->eC, o->sC, o->Cd, o->xmax, o->Sx, o->part, o->d_tiles, o->d_tob, o->err};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    delete o;
+}
+
+size_t oz_query_memory(int nbf, int naux, int max_nocc) {
+    const size_t nbf_p = (size_t)round_up(nbf, oz::MM);
+    size_t b = (size_t)naux * nbf_p * nbf_p * oz::NSL;  // int8 digits of B
+    b += (size_t)naux * nbf_p * 12;                     // row maxima and weights
+    const size_t nocc_p = (size_t)round_up(std::max(1, max_nocc), 32);
+    const size_t per_q = nocc_p * ((size_t)nbf * 8 + nbf_p * oz::NSL * 2);
+    b += std::min((size_t)naux * per_q, (size_t)x_cap_bytes() + per_q * 2048);
+    return b;
+}
+
+int oz_error_flag(OzState* o, cudaStream_t s) {
+    if (!o || !o->err) return 0;
+    int f = 0;
+    cudaMemcpyAsync(&f, o->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (f) cudaMemsetAsync(o->err, 0, sizeof(int), s);
+    return f;
+}
+
+int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int naux, const double* Cpad, int nocc,
+               int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err) {
+    using namespace oz;
+    int rc;
+    const int nbf_p = round_up(nbf, MM);
+    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
+    if (!o->err) {
+        if ((rc = oz_alloc((void**)&o->err, sizeof(int), err))) return rc;
+        cudaMemsetAsync(o->err, 0, sizeof(int), s);
+    }
+    if (!o->num_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&o->num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (o->num_sms <= 0) o->num_sms = 152;
+    }
+    if (!o->attrs_set) {
+        cudaFuncSetAttribute(oz_transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(oz_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        o->attrs_set = true;
+    }
+    // ---- digits of B (once per upload)
+    if (!o->B_ready || o->nbf_p != nbf_p) {
+        const size_t rows = (size_t)naux * nbf_p;
+        if ((rc = oz_alloc((void**)&o->rowmax, rows * 8, err)) || (rc = oz_alloc((void**)&o->sA, rows * 4, err)) ||
+            (rc = oz_alloc((void**)&o->Bd, rows * nbf_p * NSL, err)))
+            return rc;
+        cudaMemsetAsync(o->rowmax, 0, rows * 8, s);
+        if (L.ntiles > 0)
+            oz_rowmax_kernel<<<(unsigned)((size_t)naux * L.ntiles), 256, 0, s>>>(B, L.ntiles, L.tI, L.tJ, nbf_p, o->rowmax);
+        oz_split_B_kernel<<<(unsigned)((size_t)naux * nmb * nkb), 256, 0, s>>>(B, nbf, L.nT, L.ntiles, L.map, nbf_p,
+                                                                               o->rowmax, o->sA, o->Bd);
+        o->nbf_p = nbf_p;
+        o->B_ready = true;
+    }
+    // ---- digits of C^T, in column chunks of <= 80 (six accumulators in the 512 TMEM columns,
+    // three pipeline stages in shared memory)
+    const int nocc_p = nocc_pad;
+    const int nchunk = (nocc_p + TR_MAX_N - 1) / TR_MAX_N;
+    const int N = round_up((nocc_p + nchunk - 1) / nchunk, 16);
+    const int ncols = nchunk * N;
+    if ((size_t)ncols > o->sc_cap) {
+        if ((rc = oz_alloc((void**)&o->eC, ncols * sizeof(int), err)) || (rc = oz_alloc((void**)&o->sC, ncols * 4, err)))
+            return rc;
+        o->sc_cap = ncols;
+    }
+    const size_t ce = (size_t)ncols * nbf_p * NSL;
+    if (ce > o->C_cap) {
+        if ((rc = oz_alloc((void**)&o->Cd, ce * 2, err))) return rc;
+        o->C_cap = ce;
+    }
+    oz_col_scale_kernel<<<ncols, 256, 0, s>>>(Cpad, nbf, nocc_pad, nocc, o->eC, o->sC);
+    {
+        const size_t total = (size_t)ncols * (nbf_p / 8);
+        const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)o->num_sms * 8);
+        oz_split_C_kernel<<<blocks, 256, 0, s>>>(Cpad, nbf, nbf_p, nocc_pad, N, ncols, o->eC, o->Cd);
+    }
+    // ---- batches of aux functions (multiples of the group size) bounded by the X buffers
+    const int G = std::max(1, RUN_K / nocc_p);
+    const double per_q = (double)nocc_p * ((double)nbf * 8.0 + (double)nbf_p * NSL * 2.0);
+    int qb = (int)std::min<double>((double)naux, std::max<double>(G, std::floor(x_cap_bytes() / per_q / G) * G));
+    qb = std::max(1, qb);
+    if ((size_t)qb > o->X_cap) {
+        if ((rc = oz_alloc((void**)&o->Xdf, (size_t)nbf * qb * nocc_p * 8, err)) ||
+            (rc = oz_alloc((void**)&o->Xd, (size_t)nbf_p * qb * nocc_p * NSL * 2, err)))
+            return rc;
+        o->X_cap = qb;
+    }
+    const int ngroups_max = (qb + G - 1) / G;
+    if ((size_t)nbf * ngroups_max > o->xm_cap) {
+        if ((rc = oz_alloc((void**)&o->xmax, (size_t)nbf * ngroups_max * 4, err))) return rc;
+        o->xm_cap = (size_t)nbf * ngroups_max;
+    }
+    if ((size_t)nbf_p * ngroups_max > o->sx_cap) {
+        if ((rc = oz_alloc((void**)&o->Sx, (size_t)nbf_p * ngroups_max * 4, err))) return rc;
+        o->sx_cap = (size_t)nbf_p * ngroups_max;
+    }
+    // ---- contraction tiles: (128-row block, 64-row block) pairs of the lower triangle
+    if (o->tiles_nbf_p != nbf_p) {
+        const int ncb = nbf_p / CT_N;
+        std::vector<int2> tl;
+        std::vector<int> tob((size_t)nmb * ncb, -1);
+        for (int I = 0; I < nmb; ++I)
+            for (int Jc = 0; Jc < ncb && Jc * CT_N < (I + 1) * MM; ++Jc) {
+                tob[(size_t)I * ncb + Jc] = (int)tl.size();
+                tl.push_back(make_int2(I, Jc));
+            }
+        if ((rc = oz_alloc((void**)&o->d_tiles, tl.size() * sizeof(int2), err)) ||
+            (rc = oz_alloc((void**)&o->d_tob, tob.size() * sizeof(int), err)))
+            return rc;
+        cudaMemcpy(o->d_tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        cudaMemcpy(o->d_tob, tob.data(), tob.size() * sizeof(int), cudaMemcpyHostToDevice);
+        o->ntiles = (int)tl.size();
+        o->ncb = ncb;
+        o->tiles_nbf_p = nbf_p;
+    }
+    const int tr_stage = TR_OFF_C + NSL * N * MK * 2;
+    const int tr_stages = std::min(4, (SMEM_BUDGET - SMEM_RESERVE) / tr_stage);
+    const int ct_stages = std::min(4, (SMEM_BUDGET - SMEM_RESERVE) / CT_STAGE);
+    if (tr_stages < 2 || ct_stages < 2) {
+        err = "emulated FP64: pipeline stages do not fit in shared memory";
+        return GDFJK_ERR_ARG;
+    }
+    for (int q0 = 0, batch = 0; q0 < naux; q0 += qb, ++batch) {
+        const int nq = std::min(qb, naux - q0);
+        const int ngroups = (nq + G - 1) / G;
+        const size_t kdim_b = (size_t)nq * nocc_p;
+        const size_t nkbt = kdim_b / MK;
+        cudaMemsetAsync(o->xmax, 0, (size_t)nbf * ngroups * 4, s);
+        TrArgs ta{};
+        ta.Bd = o->Bd;
+        ta.Cd = o->Cd;
+        ta.sA = o->sA;
+        ta.sC = o->sC;
+        ta.Xdf = o->Xdf;
+        ta.xmax = o->xmax;
+        ta.q0 = q0;
+        ta.nq = nq;
+        ta.nmb = nmb;
+        ta.nkb = nkb;
+        ta.nbf = nbf;
+        ta.nbf_p = nbf_p;
+        ta.nocc_p = nocc_p;
+        ta.N = N;
+        ta.nchunk = nchunk;
+        ta.G = G;
+        ta.ngroups = ngroups;
+        ta.kdim_b = kdim_b;
+        ta.stages = tr_stages;
+        ta.nrun = (nkb * MK + RUN_K - 1) / RUN_K;
+        ta.run_kb = (nkb + ta.nrun - 1) / ta.nrun;
+        ta.nbuf = (2 * NACC * N <= 512) ? 2 : 1;
+        ta.tmem_cols = pow2_cols(NACC * N * ta.nbuf);
+        ta.n_items = nq * nmb * nchunk;
+        ta.err = o->err;
+        oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
+        oz_split_X_kernel<<<dim3((unsigned)nmb, (unsigned)ngroups), 256, 0, s>>>(
+            o->Xdf, o->xmax, nbf, nbf_p, ngroups, G, nq, nocc_p, kdim_b, nkbt, o->Sx, o->Xd);
+        if (ev_transform_done && q0 + qb >= naux) cudaEventRecord(ev_transform_done, s);
+        // split over groups so that there are about two work items per SM
+        int nsplit = std::max(1, std::min(ngroups, (2 * o->num_sms + o->ntiles - 1) / o->ntiles));
+        const int gps = (ngroups + nsplit - 1) / nsplit;
+        nsplit = (ngroups + gps - 1) / gps;
+        const size_t pe = (size_t)nsplit * o->ntiles * MM * CT_N;
+        if (pe > o->part_cap) {
+            if ((rc = oz_alloc((void**)&o->part, pe * 8, err))) return rc;
+            o->part_cap = pe;
+        }
+        CtArgs ca{};
+        ca.Xd = o->Xd;
+        ca.Sx = o->Sx;
+        ca.tiles = o->d_tiles;
+        ca.ntiles = o->ntiles;
+        ca.nsplit = nsplit;
+        ca.gps = gps;
+        ca.ngroups = ngroups;
+        ca.G = G;
+        ca.nocc_p = nocc_p;
+        ca.nq = nq;
+        ca.nbf_p = nbf_p;
+        ca.nkbt = nkbt;
+        ca.part = o->part;
+        ca.stages = ct_stages;
+        ca.nbuf = 1;
+        ca.n_items = o->ntiles * nsplit;
+        ca.err = o->err;
+        oz_contract_kernel<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+        const size_t nl = (size_t)nbf * (nbf + 1) / 2;
+        const int blocks = (int)std::min<size_t>((nl + 255) / 256, (size_t)o->num_sms * 16);
+        oz_reduce_kernel<<<blocks, 256, 0, s>>>(o->part, nsplit, o->ntiles, nbf, o->d_tob, o->ncb, K, batch > 0 ? 1 : 0);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("emulated FP64: launch failed: ") + cudaGetErrorString(e);
+        return GDFJK_ERR_CUDA;
+    }
+    return GDFJK_OK;
+}
+
+}  // namespace gdfjk

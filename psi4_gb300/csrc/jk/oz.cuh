@@ -1,0 +1,27 @@
+// oz.cuh — FP64-accurate exchange on the BF16 tensor cores (Ozaki-style digit splitting).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "common.cuh"
+
+namespace gdfjk {
+
+struct OzState;
+
+OzState* oz_create();
+void oz_destroy(OzState* o);
+// B changed: drop the digit copy of B.
+void oz_invalidate(OzState* o);
+// Release the digit copy of B and the X buffers (another form needs the memory).
+void oz_release(OzState* o);
+size_t oz_query_memory(int nbf, int naux, int max_nocc);
+// K (nbf x nbf, device) for the lr-symmetric density C C^T (C device, nbf_pad x nocc_pad,
+// row-major); records `ev_transform_done` after the last half-transform.
+int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int naux, const double* Cpad, int nocc,
+               int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err);
+// error bits raised by the tensor-core kernels since the last call (0 = none); clears them
+int oz_error_flag(OzState* o, cudaStream_t s);
+
+}  // namespace gdfjk

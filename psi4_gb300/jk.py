@@ -11,8 +11,9 @@ Only lr-symmetric and non-symmetric C pairs (``C_right_add``) are served, as Mem
 every compute goes through libgdfjk.so — there is no CPU path.  Errors raise
 ``GdfjkError`` (a ``RuntimeError``, as psi4's PSIEXCEPTION surfaces in Python).
 
-Extra knobs of this engine: ``set_precision("fp64" | "mixed")`` and
-``set_incremental(True)`` (mixed form: K += K(dD) over the previous build).
+Extra knobs of this engine: ``set_precision("fp64" | "fp64-emulated" | "mixed")`` and
+``set_incremental(True)`` (mixed form: K += K(dD) over the previous build).  "fp64-emulated"
+computes K to FP64 accuracy from BF16 tensor-core products of 7-bit digit slices.
 """
 from __future__ import annotations
 
@@ -228,8 +229,8 @@ class GpuDFJK:
         self.print_level = int(p)
 
     def set_precision(self, p: str):
-        if p not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if p not in ("fp64", "fp64-emulated", "mixed"):
+            raise ValueError("precision must be 'fp64', 'fp64-emulated' or 'mixed'")
         self.precision = p
 
     def set_incremental(self, v: bool):
@@ -246,7 +247,7 @@ class GpuDFJK:
         """Device bytes / 8, in doubles like psi4's JK::memory_estimate (jk.h:398)."""
         nbf = self.df.nbf if self.df is not None else self.primary.nbf
         naux = self.df.naux if self.df is not None else self.aux.nbf
-        flags = abi.MIXED if self.precision == "mixed" else 0
+        flags = {"mixed": abi.MIXED, "fp64-emulated": abi.EMULATED}.get(self.precision, 0)
         return DFJKEngine.query_memory(nbf, naux, nbf, flags) // 8
 
     def initialize(self):
@@ -293,11 +294,15 @@ class GpuDFJK:
             mode |= abi.MIXED
             if self.incremental:
                 mode |= abi.INCREMENTAL
+        emu = abi.EMULATED if (self.precision == "fp64-emulated" and lr_symmetric) else 0
+        mode |= emu
         self._J, self._K, self._D = [], [], []
-        if self.precision == "fp64" and self.incremental and lr_symmetric and self.do_K and len(self._Cl) == 1:
+        if self.precision in ("fp64", "fp64-emulated") and self.incremental and lr_symmetric and self.do_K and \
+                len(self._Cl) == 1:
             # FP64 re-anchor of the precision form: full FP64 K, kept as the incremental base
             C = self._Cl[0]
-            J, K = self.engine.compute_incremental(C, C, C.shape[1], mode=(abi.DO_J if self.do_J else 0) | abi.DO_K)
+            J, K = self.engine.compute_incremental(C, C, C.shape[1],
+                                                   mode=(abi.DO_J if self.do_J else 0) | abi.DO_K | emu)
             self._C_prev = C.copy()
             self._J.append(J if self.do_J else None)
             self._K.append(K)

@@ -98,8 +98,10 @@ class PrecisionSchedule:
        follows another FP64 build, so the final two Fock builds are full FP64 rebuilds and
        the converged energy is an FP64 energy."""
 
-    def __init__(self, anchor_d=1e-3, switch_e=1e-8, switch_d=1e-6, max_mixed=60, report_fp64=None):
+    def __init__(self, anchor_d=1e-3, switch_e=1e-8, switch_d=1e-6, max_mixed=60, report_fp64=None,
+                 fp64_precision="fp64"):
         self.anchor_d, self.switch_e, self.switch_d, self.max_mixed = anchor_d, switch_e, switch_d, max_mixed
+        self.fp64_precision = fp64_precision  # "fp64" or "fp64-emulated" for the FP64 builds
         self.report_fp64 = report_fp64  # optional JK (FP64) to measure each mixed energy's error
         self.mode = "mixed"
         self.anchored = anchor_d is None
@@ -110,10 +112,10 @@ class PrecisionSchedule:
 
     def before(self, jk):
         if self.mode == "anchor":
-            jk.set_precision("fp64")
+            jk.set_precision(self.fp64_precision)
             jk.set_incremental(True)
         else:
-            jk.set_precision(self.mode)
+            jk.set_precision("mixed" if self.mode == "mixed" else self.fp64_precision)
             jk.set_incremental(self.mode == "mixed")
 
     def after(self, dE, dnorm):

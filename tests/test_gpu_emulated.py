@@ -1,0 +1,142 @@
+"""The emulated-FP64 form on the GPU: K from BF16 tensor-core products of 7-bit digit slices
+(exact FP32 level sums, double-float epilogue) against the FP64 oracle.
+
+The digits are fixed point relative to each row's (or row group's) largest element, so the
+error scales with the magnitude of the operands rather than with each result element:
+on physical (SCF) orbitals K meets the FP64 bar of 1e-10 max absolute; on random U(0,1)
+orbitals, where |K| reaches 1e3-1e5, the bound is 1e-10 + 1e-11 max|K|."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import dfjk_ref
+from psi4_gb300 import _jkabi as abi
+from psi4_gb300.jk import DFJKEngine, GpuDFJK
+from tests.helpers import random_orbitals, reference_values, system
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+EMU = abi.DO_J | abi.DO_K | abi.EMULATED
+
+
+def _k_fp64(df, C):
+    return dfjk_ref.compute_K(df.to_pQq(), df.sparsity, C, C, df.nbf, df.naux)
+
+
+def _engine(df):
+    eng = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask)
+    eng.upload_pqq(df.to_pQq(), df.sparsity)
+    return eng
+
+
+def _scf_orbitals(name, basis):
+    from psi4_gb300.scf import core_hamiltonian, rhf
+
+    mol, pb, ab, ints, df = system(name, basis)
+    jko = dfjk_ref.OracleJK(df.to_pQq(), df.sparsity, df.nbf, df.naux)
+    nocc = mol.nelectron // 2
+    res = rhf(jko, core_hamiltonian(ints), ints.overlap(), nocc, mol.nuclear_repulsion_energy(), e_conv=1e-8,
+              d_conv=1e-6)
+    return df, res.C[:, :nocc].copy()
+
+
+def test_emulated_scf_orbitals_strict(ints_built, jk_built):
+    """(H2O)_8 cc-pVDZ converged orbitals: J and K within 1e-10 of the oracle."""
+    df, C = _scf_orbitals("h2o_8", "cc-pvdz")
+    eng = _engine(df)
+    J, K, _ = eng.compute(C, mode=EMU)
+    Jr, Kr = dfjk_ref.compute_J_symm(df.to_pQq(), df.sparsity, C @ C.T, df.nbf, df.naux), _k_fp64(df, C)
+    print(f"emulated K on SCF orbitals: max|K| {np.abs(Kr).max():.3f} max|dK| {np.abs(K - Kr).max():.2e}")
+    assert np.abs(J - Jr).max() < TOL
+    assert np.abs(K - Kr).max() < TOL
+    assert np.abs(K - K.T).max() == 0.0
+
+
+@pytest.mark.parametrize("case", [("h2o", "cc-pvdz", 1e-12), ("h2o_2", "cc-pvdz", 1e-12), ("h2o", "cc-pvtz", 1e-12),
+                                  ("h2o_2_far", "cc-pvdz", 1e-5)])
+@pytest.mark.parametrize("nocc", [5, 40, 70, 200])
+def test_emulated_random_orbitals(ints_built, jk_built, case, nocc):
+    mol, pb, ab, ints, df = system(*case)
+    eng = _engine(df)
+    C = random_orbitals(df.nbf, nocc, seed=nocc) * 0.3
+    _, K, _ = eng.compute(C, mode=EMU)
+    Kr = _k_fp64(df, C)
+    err = np.abs(K - Kr).max()
+    print(f"{case[0]}/{case[1]} nocc {nocc}: max|K| {np.abs(Kr).max():.3e} max|dK| {err:.2e}")
+    assert err < TOL + 1e-11 * np.abs(Kr).max()
+
+
+def test_emulated_determinism_and_batches(ints_built, jk_built, monkeypatch):
+    """Repeated builds are bitwise identical; cutting the aux range into many batches (tiny X
+    buffer cap) gives the same K to rounding."""
+    df, C = _scf_orbitals("h2o_8", "cc-pvdz")
+    eng = _engine(df)
+    _, K1, _ = eng.compute(C, mode=EMU)
+    _, K2, _ = eng.compute(C, mode=EMU)
+    assert np.array_equal(K1, K2)
+    monkeypatch.setenv("GDFJK_OZ_XCAP_GB", "0.002")
+    eng2 = _engine(df)
+    _, K3, _ = eng2.compute(C, mode=EMU)
+    Kr = _k_fp64(df, C)
+    print(f"batched: max|dK| {np.abs(K3 - Kr).max():.2e}, vs one batch {np.abs(K3 - K1).max():.2e}")
+    assert np.abs(K3 - Kr).max() < TOL
+    assert np.abs(K3 - K1).max() < 1e-12
+
+
+def test_emulated_long_k_runs(jk_built):
+    """nbf 1100: the half-transform's k range is cut into two exact accumulation runs.
+    Synthetic B on the device; reference: plain torch FP64."""
+    torch = pytest.importorskip("torch")
+    nbf, naux, nocc = 1100, 48, 96
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    npair = nbf * (nbf + 1) // 2
+    Bt = torch.randn((naux, npair), dtype=torch.float64, device=dev, generator=g) * 0.02
+    eng = DFJKEngine(nbf, naux, None)
+    eng.upload_device(Bt.data_ptr())
+    rows, cols = torch.tril_indices(nbf, nbf, device=dev)
+    Bd = torch.zeros((naux, nbf, nbf), dtype=torch.float64, device=dev)
+    Bd[:, rows, cols] = Bt
+    Bd[:, cols, rows] = Bt
+    C = torch.randn((nbf, nocc), dtype=torch.float64, device=dev, generator=g) * 0.1
+    X = torch.matmul(Bd, C)  # naux x nbf x nocc
+    Kr = torch.einsum("qmi,qni->mn", X, X).cpu().numpy()
+    del Bd, X
+    _, K, _ = eng.compute(C.cpu().numpy(), mode=abi.DO_K | abi.EMULATED)
+    err = np.abs(K - Kr).max()
+    print(f"nbf {nbf}: max|K| {np.abs(Kr).max():.3e} max|dK| {err:.2e}")
+    assert err < TOL + 1e-11 * np.abs(Kr).max()
+
+
+def test_emulated_scf2_energy(ints_built, jk_built):
+    """GpuDFJK with precision fp64-emulated reproduces the scf2 reference energy (1e-9)."""
+    from psi4_gb300.scf import core_hamiltonian, rhf
+
+    ref = reference_values()["scf2"]
+    mol, pb, ab, ints, df = system("h2o_scf2", "cc-pvtz")
+    jk = GpuDFJK.from_tensor(df)
+    jk.set_precision("fp64-emulated")
+    jk.initialize()
+    r = rhf(jk, core_hamiltonian(ints), ints.overlap(), mol.nelectron // 2, mol.nuclear_repulsion_energy(),
+            e_conv=1e-10, d_conv=1e-8)
+    print(f"scf2 emulated: {r.energy:.12f} ref {ref['energy']:.12f}")
+    assert abs(r.energy - ref["energy"]) < ref["tolerance"]
+
+
+def test_emulated_anchor_in_precision_schedule(ints_built, jk_built):
+    """The precision form with emulated FP64 anchors and final builds converges to the FP64
+    SCF energy."""
+    from psi4_gb300.scf import PrecisionSchedule, core_hamiltonian, rhf
+
+    mol, pb, ab, ints, df = system("h2o_8", "cc-pvdz")
+    args = (core_hamiltonian(ints), ints.overlap(), 40, mol.nuclear_repulsion_energy())
+    jk64 = GpuDFJK.from_tensor(df)
+    jk64.initialize()
+    e64 = rhf(jk64, *args, e_conv=1e-10, d_conv=1e-8).energy
+    jk = GpuDFJK.from_tensor(df)
+    jk.initialize()
+    r = rhf(jk, *args, e_conv=1e-10, d_conv=1e-8, schedule=PrecisionSchedule(fp64_precision="fp64-emulated"))
+    print(f"schedule with emulated FP64 builds: {r.energy:.12f} vs FP64 {e64:.12f}")
+    assert abs(r.energy - e64) < 1e-9
