@@ -1177,9 +1177,10 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         ta.n_items = nq * nmb * nchunk;
         ta.err = o->err;
         oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
+        // the transform phase ends with the last batch's half-transform kernel
+        if (ev_transform_done && q0 + qb >= naux) cudaEventRecord(ev_transform_done, s);
         oz_split_X_kernel<<<dim3((unsigned)nmb, (unsigned)ngroups), 256, 0, s>>>(
             o->Xdf, o->xmax, nbf, nbf_p, ngroups, G, nq, nocc_p, kdim_b, nkbt, o->Sx, o->Xd);
-        if (ev_transform_done && q0 + qb >= naux) cudaEventRecord(ev_transform_done, s);
         // split over groups so that there are about two work items per SM
         int nsplit = std::max(1, std::min(ngroups, (2 * o->num_sms + o->ntiles - 1) / o->ntiles));
         const int gps = (ngroups + nsplit - 1) / nsplit;
