@@ -64,11 +64,12 @@ constexpr int MAX_A_SLOTS = 3;               // A slices per pass, at most
 constexpr int E_EMPTY = -100000;             // exponent of an all-zero row
 constexpr int SMEM_BUDGET = 224 * 1024;
 constexpr int SMEM_RESERVE = 2048;
-constexpr int TR_THREADS = 320;              // producer, MMA, 4 epilogue warps, 4 converter warps
+constexpr int TR_THREADS = 448;              // producer, MMA, 8 epilogue warps, 4 converter warps
 constexpr int CT_THREADS = 192;              // producer, MMA, 4 epilogue warps
 constexpr int CT_N = 64;                     // contraction tile columns
 constexpr int TR_MAX_N = 80;                 // half-transform accumulator columns
-constexpr int RUN_K = 1024;                  // terms per exact accumulation run
+constexpr int RUN_K = 1024;                  // contraction terms per accumulation run (levels 0-3 exact)
+constexpr int TR_RUN_K = 2048;               // half-transform terms per run (levels 0-1 exact for any digits)
 static_assert(tc::SWZ == 64, "digit slices are laid out for the 64-byte swizzle");
 
 // the three passes: first A slice, A slices, B slices
@@ -389,13 +390,19 @@ struct TrArgs {
     int q0, nq, nmb, nkb, nbf, nbf_p, nocc_p, N, nchunk, G, ngroups;
     int run_kb, nrun;          // k blocks per accumulation run, runs per item
     size_t kdim_b;
-    int stages, nbuf, tmem_cols, n_items;
+    int stages, nbuf, n_items, ncols;
     int* err;
 };
 
-constexpr int TR_OFF_I8 = 0;                                  // <= 3 int8 slices of A (12 KB)
-constexpr int TR_OFF_BF = MAX_A_SLOTS * I8_SLICE;             // <= 3 BF16 slices of A (24 KB)
-constexpr int TR_OFF_C = TR_OFF_BF + MAX_A_SLOTS * BF_SLICE;  // <= 7 BF16 slices of C^T (N rows)
+// The half-transform keeps its A operand (the digit slices of B) in tensor memory: the
+// converter warps write each converted slice straight into one of TR_ASLOTS 16-column TMEM
+// slots with tcgen05.st, and the MMAs read A from there (only C^T comes from shared memory).
+// Its accumulators: levels 0-3 exact and a tail (4-6); the round-toward-zero truncation of
+// the tail is harmless here (no sums of squares; it is random relative to X).
+constexpr int TR_NACC = 5;
+constexpr int TR_ASLOTS = 4;
+constexpr int TR_ACOL0 = 512 - TR_ASLOTS * 16;  // first A-slot column
+constexpr int TR_OFF_C = NSL * I8_SLICE;        // stage: [7 int8 A slices | 7 BF16 C^T slices]
 
 __device__ __forceinline__ void tr_item(const TrArgs& a, int item, int& Q, int& mb, int& chunk) {
     chunk = item % a.nchunk;
@@ -408,10 +415,57 @@ __device__ __forceinline__ void tr_run(const TrArgs& a, int run, int& kb0, int& 
     kb1 = min(a.nkb, kb0 + a.run_kb);
 }
 
-// Persistent, warp-specialised: warp 0 lane 0 bulk-copies int8 A and BF16 C^T slices into a
-// ring of stages; warps 6-9 convert the int8 digit fields to BF16 slice values in the stage;
-// warp 1 lane 0 issues the slice-pair MMAs into six accumulators; warps 2-5 drain them
-// (tcgen05.ld) after every run into double-float X, and take the per-group row maxima.
+// a[0] + ... + a[4]: four exact level sums and the tail, as an FP32 pair
+__device__ __forceinline__ void combine5(const float* a, float& hi, float& lo) {
+    float s, e1, e2, e3;
+    two_sum(a[0], a[1], s, e1);
+    two_sum(s, a[2], s, e2);
+    two_sum(s, a[3], s, e3);
+    const float l = __fadd_rn(__fadd_rn(__fadd_rn(e1, e2), e3), a[4]);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
+}
+
+// MMA with the A operand in tensor memory
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// one A slice (slot at TMEM column a_col) against the C^T slices of the stage: pairs (J, t),
+// t <= 6 - J, into accumulator min(J + t, 4); `first` starts a fresh accumulation run
+template <int J>
+__device__ __forceinline__ void issue_slice(const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step, uint32_t id,
+                                            bool first) {
+#pragma unroll
+    for (int ks = 0; ks < MK / 16; ++ks) {
+#pragma unroll
+        for (int t = 0; t <= NSL - 1 - J; ++t) {
+            const int L = J + t < TR_NACC - 1 ? J + t : TR_NACC - 1;
+            const uint32_t f = (first && ks == 0 && J == 0 && t <= TR_NACC - 1) ? 0u : 1u;
+            mma_bf16_ta(d[L], a_col + (uint32_t)(8 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
+        }
+    }
+}
+
+// Persistent, warp-specialised: warp 0 lane 0 bulk-copies one k block (int8 A + BF16 C^T) per
+// stage; warps 6-9 convert A slice by slice into TMEM slots (each thread its own row);
+// warp 1 lane 0 issues the slice-pair MMAs; warps 2-5 drain the accumulators (tcgen05.ld)
+// after every run into double-float X and take the row maxima.
 __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -419,122 +473,138 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
     const int c_slice = N * MK * 2;
     const int stage_bytes = TR_OFF_C + NSL * c_slice;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * stage_bytes);
-    uint64_t* conv = full + a.stages;
-    uint64_t* empty = conv + a.stages;
-    uint64_t* tfull = empty + a.stages;  // [2]
-    uint64_t* tempty = tfull + 2;        // [2]
+    uint64_t* empty = full + a.stages;
+    uint64_t* afull = empty + a.stages;   // [TR_ASLOTS]
+    uint64_t* aempty = afull + TR_ASLOTS; // [TR_ASLOTS]
+    uint64_t* tfull = aempty + TR_ASLOTS; // [2]
+    uint64_t* tempty = tfull + 2;         // [2]
     uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+    float* s_sc = reinterpret_cast<float*>(tmem_holder + 4);  // slice weights of the columns of C
     const int warp = threadIdx.x / 32;
+    for (int i = threadIdx.x; i < a.ncols; i += blockDim.x) s_sc[i] = a.sC[i];
     if (threadIdx.x == 0) {
         for (int s = 0; s < a.stages; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&conv[s], 128);
             tc::mbar_init(&empty[s], 1);
+        }
+        for (int r = 0; r < TR_ASLOTS; ++r) {
+            tc::mbar_init(&afull[r], 128);
+            tc::mbar_init(&aempty[r], 1);
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&tfull[b], 1);
-            tc::mbar_init(&tempty[b], 4);
+            tc::mbar_init(&tempty[b], 8);
         }
         *abort_flag = 0;
         tc::fence_barrier_init();
     }
-    if (warp == 0) tc::tmem_alloc(tmem_holder, (uint32_t)a.tmem_cols);
+    if (warp == 0) tc::tmem_alloc(tmem_holder, 512u);
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_holder;
 
     if (threadIdx.x == 0) {
-        // ---- producer
+        // ---- producer: one stage per k block
         int s = 0;
         uint32_t ph = 0;
         long kg = 0;
         bool ok = true;
+        const uint32_t cbytes = (uint32_t)(NSL * c_slice);
         for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
             int Q, mb, chunk;
             tr_item(a, item, Q, mb, chunk);
             const uint8_t* pa = a.Bd + ((size_t)Q * a.nmb + mb) * a.nkb * I8_BLOCK;
             const __nv_bfloat16* pc = a.Cd + (size_t)chunk * a.nkb * NSL * N * MK;
-            for (int run = 0; ok && run < a.nrun; ++run) {
-                int kb0, kb1;
-                tr_run(a, run, kb0, kb1);
-                for (int pass = 0; ok && pass < NPASS; ++pass) {
-                    const uint32_t ab = (uint32_t)(pass_na(pass) * I8_SLICE);
-                    const uint32_t cb = (uint32_t)(pass_nb(pass) * c_slice);
-                    for (int kb = kb0; kb < kb1; ++kb, ++kg) {
-                        if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
-                            ok = false;
-                            break;
-                        }
-                        uint8_t* st = smem + (size_t)s * stage_bytes;
-                        tc::mbar_arrive_expect_tx(&full[s], ab + cb);
-                        tc::bulk_load(st + TR_OFF_I8, pa + (size_t)kb * I8_BLOCK + pass_a0(pass) * I8_SLICE, ab, &full[s]);
-                        tc::bulk_load(st + TR_OFF_C, pc + (size_t)kb * NSL * N * MK, cb, &full[s]);
-                        if (++s == a.stages) {
-                            s = 0;
-                            ph ^= 1u;
-                        }
-                    }
+            for (int kb = 0; kb < a.nkb; ++kb, ++kg) {
+                if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = smem + (size_t)s * stage_bytes;
+                tc::mbar_arrive_expect_tx(&full[s], (uint32_t)I8_BLOCK + cbytes);
+                tc::bulk_load(st, pa + (size_t)kb * I8_BLOCK, (uint32_t)I8_BLOCK, &full[s]);
+                tc::bulk_load(st + TR_OFF_C, pc + (size_t)kb * NSL * N * MK, cbytes, &full[s]);
+                if (++s == a.stages) {
+                    s = 0;
+                    ph ^= 1u;
                 }
             }
         }
-    } else if (warp >= 6) {
-        // ---- converters: int8 fields (d + 64) -> BF16 (d * 2^(-7 slice)), swizzled K-major
-        const int ct = threadIdx.x - 192;
-        int s = 0;
-        uint32_t ph = 0;
+    } else if (warp >= 6 && warp < 10) {
+        // ---- converters: row `row` of every slice, int8 field (d + 64) -> BF16 d * 2^(-7 slice),
+        // two K elements per 32-bit TMEM column, into the next A slots, two slices per step
+        const int q = warp % 4;
+        const int row = q * 32 + (threadIdx.x % 32);
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        int s = 0, r = 0;
+        uint32_t ph = 0, pr = 0;
+        long used = 0;
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
-            for (int run = 0; ok && run < a.nrun; ++run) {
-                int kb0, kb1;
-                tr_run(a, run, kb0, kb1);
-                for (int pass = 0; ok && pass < NPASS; ++pass) {
-                    const int units = pass_na(pass) * MM * (MK / 8);
-                    for (int kb = kb0; kb < kb1; ++kb) {
-                        if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+            for (int kb = 0; ok && kb < a.nkb; ++kb) {
+                if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                    ok = false;
+                    break;
+                }
+                const uint8_t* st = smem + (size_t)s * stage_bytes;
+#pragma unroll 1
+                for (int j0 = 0; ok && j0 < NSL; j0 += 2) {
+                    const int nj = NSL - j0 < 2 ? NSL - j0 : 2;
+                    int slot[2] = {0, 0};
+                    for (int jj = 0; jj < nj; ++jj, ++used) {
+                        if (used >= TR_ASLOTS && !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
                             ok = false;
                             break;
                         }
-                        uint8_t* st = smem + (size_t)s * stage_bytes;
-                        for (int u = ct; u < units; u += 128) {
-                            const int j = u / (MM * (MK / 8));
-                            const int rem = u % (MM * (MK / 8));
-                            const int r = rem / (MK / 8), c = rem % (MK / 8);
-                            const uint2 q = *reinterpret_cast<const uint2*>(st + TR_OFF_I8 + j * I8_SLICE + r * MK + c * 8);
-                            const float w = slice_weight(pass_a0(pass) + j);
-                            const float off = -8388672.0f * w;
-                            uint32_t o[4];
-#pragma unroll
-                            for (int h = 0; h < 4; ++h) {
-                                const uint32_t word = h < 2 ? q.x : q.y;
-                                const uint32_t b0 = __byte_perm(word, 0x4B000000u, 0x7440u | (uint32_t)((2 * h) % 4));
-                                const uint32_t b1 = __byte_perm(word, 0x4B000000u, 0x7440u | (uint32_t)((2 * h + 1) % 4));
-                                const float g0 = fmaf(__uint_as_float(b0), w, off);
-                                const float g1 = fmaf(__uint_as_float(b1), w, off);
-                                o[h] = __byte_perm(__float_as_uint(g0), __float_as_uint(g1), 0x7632u);
-                            }
-                            *reinterpret_cast<uint4*>(st + TR_OFF_BF + j * BF_SLICE +
-                                                      tc::swz_offset((uint32_t)r, (uint32_t)c)) = make_uint4(o[0], o[1], o[2], o[3]);
-                        }
-                        fence_proxy_async();
-                        tc::mbar_arrive(&conv[s]);
-                        if (++s == a.stages) {
-                            s = 0;
-                            ph ^= 1u;
+                        slot[jj] = r;
+                        if (++r == TR_ASLOTS) {
+                            r = 0;
+                            pr ^= 1u;
                         }
                     }
+                    if (!ok) break;
+                    tc::tc_fence_after();
+                    for (int jj = 0; jj < nj; ++jj) {
+                        const int j = j0 + jj;
+                        const uint4 q0 = *reinterpret_cast<const uint4*>(st + j * I8_SLICE + row * MK);
+                        const uint4 q1 = *reinterpret_cast<const uint4*>(st + j * I8_SLICE + row * MK + 16);
+                        const uint32_t words[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+                        const float w = slice_weight(j);
+                        const float off = -8388672.0f * w;
+                        uint32_t o[16];
+#pragma unroll
+                        for (int wi = 0; wi < 8; ++wi) {
+#pragma unroll
+                            for (int hh = 0; hh < 2; ++hh) {
+                                const uint32_t b0 = __byte_perm(words[wi], 0x4B000000u, 0x7440u | (uint32_t)(2 * hh));
+                                const uint32_t b1 = __byte_perm(words[wi], 0x4B000000u, 0x7440u | (uint32_t)(2 * hh + 1));
+                                const float g0 = fmaf(__uint_as_float(b0), w, off);
+                                const float g1 = fmaf(__uint_as_float(b1), w, off);
+                                o[2 * wi + hh] = __byte_perm(__float_as_uint(g0), __float_as_uint(g1), 0x7632u);
+                            }
+                        }
+                        tmem_st16(lane_base + (uint32_t)(TR_ACOL0 + 16 * slot[jj]), o);
+                    }
+                    tmem_wait_st();
+                    tc::tc_fence_before();
+                    for (int jj = 0; jj < nj; ++jj) tc::mbar_arrive(&afull[slot[jj]]);
+                }
+                if (++s == a.stages) {
+                    s = 0;
+                    ph ^= 1u;
                 }
             }
         }
     } else if (threadIdx.x == 32) {
-        // ---- MMA issuer
-        int s = 0;
-        uint32_t ph = 0;
-        int ri = 0;  // accumulation runs issued by this CTA
+        // ---- MMA issuer: per k block, seven A slices from TMEM slots against one stage
+        int s = 0, r = 0;
+        uint32_t ph = 0, pr = 0;
+        int ri = 0;
         const uint32_t smem_base = tc::smem_u32(smem);
         const uint32_t id = tc::idesc_bf16_f32(MM, N, false);
-        const uint64_t a_step = (uint64_t)(BF_SLICE >> 4), b_step = (uint64_t)(c_slice >> 4);
+        const uint64_t b_step = (uint64_t)(c_slice >> 4);
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
             for (int run = 0; ok && run < a.nrun; ++run, ++ri) {
@@ -544,48 +614,65 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t d0 = tmem + (uint32_t)(buf * NACC * N);
-                uint32_t d[NACC];
+                const uint32_t d0 = tmem + (uint32_t)(buf * TR_NACC * N);
+                uint32_t d[TR_NACC];
 #pragma unroll
-                for (int L = 0; L < NACC; ++L) d[L] = d0 + (uint32_t)(L * N);
+                for (int L = 0; L < TR_NACC; ++L) d[L] = d0 + (uint32_t)(L * N);
                 int kb0, kb1;
                 tr_run(a, run, kb0, kb1);
-                for (int pass = 0; ok && pass < NPASS; ++pass) {
-                    for (int kb = kb0; kb < kb1; ++kb) {
-                        if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err) ||
-                            !tc::mbar_wait(&conv[s], ph, abort_flag, a.err)) {
+                for (int kb = kb0; ok && kb < kb1; ++kb) {
+                    if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint64_t dB = tc::sdesc_kmajor(smem_base + (uint32_t)(s * stage_bytes + TR_OFF_C));
+                    const bool first = kb == kb0;
+#pragma unroll
+                    for (int j = 0; j < NSL; ++j) {
+                        if (!tc::mbar_wait(&afull[r], pr, abort_flag, a.err)) {
                             ok = false;
                             break;
                         }
                         tc::tc_fence_after();
-                        const uint32_t st = smem_base + (uint32_t)(s * stage_bytes);
-                        const uint64_t dA = tc::sdesc_kmajor(st + TR_OFF_BF), dB = tc::sdesc_kmajor(st + TR_OFF_C);
-#pragma unroll
-                        for (int ks = 0; ks < MK / 16; ++ks) {
-                            const uint64_t ko = (uint64_t)(2 * ks);
-                            issue_pairs(pass, d, dA + ko, dB + ko, a_step, b_step, id, (pass | (kb - kb0) | ks) != 0 ? 1u : 0u);
+                        const uint32_t a_col = tmem + (uint32_t)(TR_ACOL0 + 16 * r);
+                        switch (j) {
+                            case 0: issue_slice<0>(d, a_col, dB, b_step, id, first); break;
+                            case 1: issue_slice<1>(d, a_col, dB, b_step, id, first); break;
+                            case 2: issue_slice<2>(d, a_col, dB, b_step, id, first); break;
+                            case 3: issue_slice<3>(d, a_col, dB, b_step, id, first); break;
+                            case 4: issue_slice<4>(d, a_col, dB, b_step, id, first); break;
+                            case 5: issue_slice<5>(d, a_col, dB, b_step, id, first); break;
+                            default: issue_slice<6>(d, a_col, dB, b_step, id, first); break;
                         }
-                        tc::mma_commit(&empty[s]);
-                        if (++s == a.stages) {
-                            s = 0;
-                            ph ^= 1u;
+                        tc::mma_commit(&aempty[r]);
+                        if (++r == TR_ASLOTS) {
+                            r = 0;
+                            pr ^= 1u;
                         }
+                    }
+                    if (!ok) break;
+                    tc::mma_commit(&empty[s]);
+                    if (++s == a.stages) {
+                        s = 0;
+                        ph ^= 1u;
                     }
                 }
                 tc::mma_commit(&tfull[buf]);
             }
         }
     } else if (warp >= 2) {
-        // ---- epilogue: after each run, X (+)= run sum; after the last, the row maximum
+        // ---- epilogue (warps 2-5 and 10-13, one column half each): after each run,
+        // X (+)= run sum; after the last, the row maximum
         const int q = warp % 4;
-        const int r = q * 32 + (threadIdx.x % 32);
+        const int half = warp >= 10 ? 1 : 0;
+        const int rr = q * 32 + (threadIdx.x % 32);
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
         int ri = 0;
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
             int Q, mb, chunk;
             tr_item(a, item, Q, mb, chunk);
-            const int m = mb * MM + r;
+            const int m = mb * MM + rr;
             const bool valid = m < a.nbf;
             const float sa = valid ? a.sA[(size_t)Q * a.nbf_p + m] : 0.f;
             float2* xrow = a.Xdf + (valid ? (size_t)m * a.kdim_b + (size_t)(Q - a.q0) * a.nocc_p : 0);
@@ -599,29 +686,34 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t cb = lane_base + (uint32_t)(buf * NACC * N);
+                const uint32_t cb = lane_base + (uint32_t)(buf * TR_NACC * N);
                 const bool last = run == a.nrun - 1;
-                for (int c0 = 0; c0 < N; c0 += 8) {
-                    uint32_t v[NACC][8];
-#pragma unroll
-                    for (int L = 0; L < NACC; ++L) tc::tmem_ld8(cb + (uint32_t)(L * N + c0), v[L]);
+                for (int c0 = half * (N / 2); c0 < (half + 1) * (N / 2); c0 += 8) {
                     const int i0 = chunk * N + c0;
+                    float2 prev[8];
+                    if (run > 0 && valid) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) prev[j] = i0 + j < a.nocc_p ? xrow[i0 + j] : make_float2(0.f, 0.f);
+                    }
+                    uint32_t v[TR_NACC][8];
+#pragma unroll
+                    for (int L = 0; L < TR_NACC; ++L) tc::tmem_ld8_nowait(cb + (uint32_t)(L * N + c0), v[L]);
+                    tc::tmem_wait_ld();
                     if (valid) {
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
                             const int i = i0 + j;
                             if (i < a.nocc_p) {
-                                float acc[NACC];
+                                float acc[TR_NACC];
 #pragma unroll
-                                for (int L = 0; L < NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
+                                for (int L = 0; L < TR_NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
                                 float hi, lo;
-                                combine6(acc, hi, lo);
-                                const float sc = sa * a.sC[i];
+                                combine5(acc, hi, lo);
+                                const float sc = sa * s_sc[i];
                                 hi *= sc;
                                 lo *= sc;
                                 if (run > 0) {
-                                    const float2 prev = xrow[i];
-                                    float H = prev.x, Lo = prev.y;
+                                    float H = prev[j].x, Lo = prev[j].y;
                                     df_add(H, Lo, hi, lo);
                                     hi = H;
                                     lo = Lo;
@@ -649,7 +741,7 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
     }
     tc::tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+    if (warp == 0) tc::tmem_dealloc(tmem, 512u);
 }
 
 // ---------------------------------------------------------------- split of X
@@ -981,12 +1073,6 @@ void oz_free(void** p) {
     *p = nullptr;
 }
 
-int pow2_cols(int n) {
-    int c = 32;
-    while (c < n) c <<= 1;
-    return c;
-}
-
 double x_cap_bytes() {
     const char* s = getenv("GDFJK_OZ_XCAP_GB");
     double gb = s ? atof(s) : 24.0;
@@ -1138,7 +1224,7 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         o->tiles_nbf_p = nbf_p;
     }
     const int tr_stage = TR_OFF_C + NSL * N * MK * 2;
-    const int tr_stages = std::min(4, (SMEM_BUDGET - SMEM_RESERVE) / tr_stage);
+    const int tr_stages = std::min(4, (SMEM_BUDGET - SMEM_RESERVE - 4 * ncols) / tr_stage);
     const int ct_stages = std::min(4, (SMEM_BUDGET - SMEM_RESERVE) / CT_STAGE);
     if (tr_stages < 2 || ct_stages < 2) {
         err = "emulated FP64: pipeline stages do not fit in shared memory";
@@ -1170,10 +1256,10 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         ta.ngroups = ngroups;
         ta.kdim_b = kdim_b;
         ta.stages = tr_stages;
-        ta.nrun = (nkb * MK + RUN_K - 1) / RUN_K;
+        ta.nrun = (nkb * MK + TR_RUN_K - 1) / TR_RUN_K;
+        ta.ncols = ncols;
         ta.run_kb = (nkb + ta.nrun - 1) / ta.nrun;
-        ta.nbuf = (2 * NACC * N <= 512) ? 2 : 1;
-        ta.tmem_cols = pow2_cols(NACC * N * ta.nbuf);
+        ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;
         ta.n_items = nq * nmb * nchunk;
         ta.err = o->err;
         oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
