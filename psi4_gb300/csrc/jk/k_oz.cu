@@ -23,19 +23,19 @@
 // double-float (FP32 pairs).
 //
 //   half-transform   X[m][(Q,i)] = sum_n B_Q[m][n] C[n][i]      A = digits of B (int8 in HBM,
-//                    converted to BF16 slices in shared memory by four converter warps),
-//                    B = digits of C^T (BF16); one item = (Q, 128 rows, a chunk of <= 80
-//                    columns), k split into runs of <= 1024; X out in double-float plus a
-//                    row max per group of Q.
+//                    converted to BF16 slice values by four converter warps that write them
+//                    straight into tensor memory), B = digits of C^T (BF16, shared memory);
+//                    one item = (Q, 128 rows, a chunk of <= 80 columns), k in runs of <= 2048;
+//                    X out in double-float plus a row max per group of Q.
 //   split            X -> BF16 digit slices with one exponent per (row, group of Q), a group
 //                    being <= 1024 contraction terms.
 //   contraction      K[m][n] = sum_groups 2^(E_m+E_n-10) sum_pairs ... : 128 x 64 tiles of the
-//                    lower triangle; one accumulation run per group, drained into a
-//                    double-float running sum in registers; split over groups; FP64 partials
-//                    summed in a fixed order.
-// Each accumulation run covers its k range in three passes (A slices {0,1} with B slices
-// 0-6, {2,3} with 0-4, {4,5,6} with 0-2) so that one pipeline stage holds at most three
-// A slices and seven B slices.
+//                    lower triangle; A slices copied into tensor memory by four copier warps;
+//                    one accumulation run per group, drained into a double-float running sum
+//                    in registers; split over groups; FP64 partials summed in a fixed order.
+// In both GEMMs one pipeline stage holds every digit slice of one 32-deep k block, and the
+// MMA issuer walks the A slices j = 0..6 (each from its TMEM slot) against B slices
+// t = 0..6-j, accumulator min(j + t, last).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -56,26 +56,18 @@ constexpr int MM = 128;                      // tile rows (MMA M)
 constexpr int MK = 32;                       // k per pipeline stage (one 64-byte row of BF16)
 constexpr int NSL = 7;                       // digit slices
 constexpr int NACC = 6;                      // accumulators: levels 0..4 and the tail (5, 6)
-constexpr int NPASS = 3;
 constexpr int I8_SLICE = MM * MK;            // bytes of one int8 digit slice of a 128 x 32 block
 constexpr int BF_SLICE = MM * MK * 2;        // bytes of one BF16 slice of a 128 x 32 block
 constexpr int I8_BLOCK = NSL * I8_SLICE;     // 28 KB: all slices of one 128 x 32 block of B
-constexpr int MAX_A_SLOTS = 3;               // A slices per pass, at most
 constexpr int E_EMPTY = -100000;             // exponent of an all-zero row
 constexpr int SMEM_BUDGET = 224 * 1024;
 constexpr int SMEM_RESERVE = 2048;
 constexpr int TR_THREADS = 448;              // producer, MMA, 8 epilogue warps, 4 converter warps
-constexpr int CT_THREADS = 192;              // producer, MMA, 4 epilogue warps
 constexpr int CT_N = 64;                     // contraction tile columns
 constexpr int TR_MAX_N = 80;                 // half-transform accumulator columns
 constexpr int RUN_K = 1024;                  // contraction terms per accumulation run (levels 0-3 exact)
 constexpr int TR_RUN_K = 2048;               // half-transform terms per run (levels 0-1 exact for any digits)
 static_assert(tc::SWZ == 64, "digit slices are laid out for the 64-byte swizzle");
-
-// the three passes: first A slice, A slices, B slices
-__host__ __device__ __forceinline__ constexpr int pass_a0(int p) { return p == 0 ? 0 : (p == 1 ? 2 : 4); }
-__host__ __device__ __forceinline__ constexpr int pass_na(int p) { return p == 2 ? 3 : 2; }
-__host__ __device__ __forceinline__ constexpr int pass_nb(int p) { return p == 0 ? 7 : (p == 1 ? 5 : 3); }
 
 // offset added to v so that every base-128 digit field of u = v + OFF is d_s + 64 in [0, 127]
 constexpr unsigned long long DIGIT_OFF =
@@ -337,48 +329,6 @@ __device__ __forceinline__ void df_add(float& H, float& L, float hi, float lo) {
     L = __fsub_rn(l, __fsub_rn(H, s));
 }
 
-// The slice pairs of one 16-deep k step of pass `pass` (A slot j = slice pass_a0 + j, B slot
-// t = slice t).  d[L] accumulates level L = 0..4, d[5] the tail (levels 5, 6); `f` = 0 starts
-// a fresh accumulation run (every accumulator is first written in pass 0).
-__device__ __forceinline__ void issue_pairs(int pass, const uint32_t* d, uint64_t a0, uint64_t b0, uint64_t a_step,
-                                            uint64_t b_step, uint32_t id, uint32_t f) {
-    const uint64_t a1 = a0 + a_step, a2 = a0 + 2 * a_step;
-    const uint64_t b1 = b0 + b_step, b2 = b0 + 2 * b_step, b3 = b0 + 3 * b_step, b4 = b0 + 4 * b_step;
-    if (pass == 0) {  // slices 0, 1 x 0..6
-        const uint64_t b5 = b0 + 5 * b_step, b6 = b0 + 6 * b_step;
-        tc::mma_bf16(d[0], a0, b0, id, f);
-        tc::mma_bf16(d[1], a0, b1, id, f);
-        tc::mma_bf16(d[1], a1, b0, id, 1u);
-        tc::mma_bf16(d[2], a0, b2, id, f);
-        tc::mma_bf16(d[2], a1, b1, id, 1u);
-        tc::mma_bf16(d[3], a0, b3, id, f);
-        tc::mma_bf16(d[3], a1, b2, id, 1u);
-        tc::mma_bf16(d[4], a0, b4, id, f);
-        tc::mma_bf16(d[4], a1, b3, id, 1u);
-        tc::mma_bf16(d[5], a0, b5, id, f);
-        tc::mma_bf16(d[5], a1, b4, id, 1u);
-        tc::mma_bf16(d[5], a0, b6, id, 1u);
-        tc::mma_bf16(d[5], a1, b5, id, 1u);
-    } else if (pass == 1) {  // slices 2, 3 x 0..4
-        tc::mma_bf16(d[2], a0, b0, id, 1u);
-        tc::mma_bf16(d[3], a0, b1, id, 1u);
-        tc::mma_bf16(d[3], a1, b0, id, 1u);
-        tc::mma_bf16(d[4], a0, b2, id, 1u);
-        tc::mma_bf16(d[4], a1, b1, id, 1u);
-        tc::mma_bf16(d[5], a0, b3, id, 1u);
-        tc::mma_bf16(d[5], a1, b2, id, 1u);
-        tc::mma_bf16(d[5], a0, b4, id, 1u);
-        tc::mma_bf16(d[5], a1, b3, id, 1u);
-    } else {  // slices 4, 5, 6 x 0..2
-        tc::mma_bf16(d[4], a0, b0, id, 1u);
-        tc::mma_bf16(d[5], a0, b1, id, 1u);
-        tc::mma_bf16(d[5], a1, b0, id, 1u);
-        tc::mma_bf16(d[5], a0, b2, id, 1u);
-        tc::mma_bf16(d[5], a1, b1, id, 1u);
-        tc::mma_bf16(d[5], a2, b0, id, 1u);
-    }
-}
-
 // ---------------------------------------------------------------- half-transform
 struct TrArgs {
     const uint8_t* Bd;         // int8 digit fields of B, [Q][mb][kb][7][128][32]
@@ -448,17 +398,32 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 
 // one A slice (slot at TMEM column a_col) against the C^T slices of the stage: pairs (J, t),
 // t <= 6 - J, into accumulator min(J + t, 4); `first` starts a fresh accumulation run
-template <int J>
+template <int NA, int J>
 __device__ __forceinline__ void issue_slice(const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step, uint32_t id,
                                             bool first) {
 #pragma unroll
     for (int ks = 0; ks < MK / 16; ++ks) {
 #pragma unroll
         for (int t = 0; t <= NSL - 1 - J; ++t) {
-            const int L = J + t < TR_NACC - 1 ? J + t : TR_NACC - 1;
-            const uint32_t f = (first && ks == 0 && J == 0 && t <= TR_NACC - 1) ? 0u : 1u;
+            const int L = J + t < NA - 1 ? J + t : NA - 1;
+            const uint32_t f = (first && ks == 0 && J == 0 && t <= NA - 1) ? 0u : 1u;
             mma_bf16_ta(d[L], a_col + (uint32_t)(8 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
         }
+    }
+}
+
+// slice j (0..6) of the A operand from its TMEM slot: the (7 - j) pairs with B slices 0..6-j
+template <int NA>
+__device__ __forceinline__ void issue_slice_j(int j, const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step,
+                                              uint32_t id, bool first) {
+    switch (j) {
+        case 0: issue_slice<NA, 0>(d, a_col, dB, b_step, id, first); break;
+        case 1: issue_slice<NA, 1>(d, a_col, dB, b_step, id, first); break;
+        case 2: issue_slice<NA, 2>(d, a_col, dB, b_step, id, first); break;
+        case 3: issue_slice<NA, 3>(d, a_col, dB, b_step, id, first); break;
+        case 4: issue_slice<NA, 4>(d, a_col, dB, b_step, id, first); break;
+        case 5: issue_slice<NA, 5>(d, a_col, dB, b_step, id, first); break;
+        default: issue_slice<NA, 6>(d, a_col, dB, b_step, id, first); break;
     }
 }
 
@@ -635,15 +600,7 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                         }
                         tc::tc_fence_after();
                         const uint32_t a_col = tmem + (uint32_t)(TR_ACOL0 + 16 * r);
-                        switch (j) {
-                            case 0: issue_slice<0>(d, a_col, dB, b_step, id, first); break;
-                            case 1: issue_slice<1>(d, a_col, dB, b_step, id, first); break;
-                            case 2: issue_slice<2>(d, a_col, dB, b_step, id, first); break;
-                            case 3: issue_slice<3>(d, a_col, dB, b_step, id, first); break;
-                            case 4: issue_slice<4>(d, a_col, dB, b_step, id, first); break;
-                            case 5: issue_slice<5>(d, a_col, dB, b_step, id, first); break;
-                            default: issue_slice<6>(d, a_col, dB, b_step, id, first); break;
-                        }
+                        issue_slice_j<TR_NACC>(j, d, a_col, dB, b_step, id, first);
                         tc::mma_commit(&aempty[r]);
                         if (++r == TR_ASLOTS) {
                             r = 0;
@@ -803,12 +760,19 @@ struct CtArgs {
     int ntiles, nsplit, gps, ngroups, G, nocc_p, nq, nbf_p;
     size_t nkbt;
     double* part;  // [nsplit][ntiles][128][64]
-    int stages, nbuf, n_items;
+    int stages, n_items;
     int* err;
 };
 
-constexpr int CT_OFF_B = MAX_A_SLOTS * BF_SLICE;          // A: <= 3 slices of 128 rows (24 KB)
-constexpr int CT_STAGE = CT_OFF_B + NSL * CT_N * MK * 2;  // B: <= 7 slices of 64 rows (28 KB)
+// Stage per k block: [7 A slices, 128 rows | 7 B slices, 64 rows].  The copier warps move each
+// A slice into a TMEM slot (the MMAs take A from tensor memory and only B from shared memory);
+// six accumulators (levels 0-4 exact, tail 5-6) at TMEM columns 0..383, A slots at 448..511.
+constexpr int CT_NACC = NACC;
+constexpr int CT_OFF_B = NSL * BF_SLICE;                  // 56 KB
+constexpr int CT_STAGE = CT_OFF_B + NSL * CT_N * MK * 2;  // + 28 KB
+constexpr int CT_ASLOTS = 4;
+constexpr int CT_ACOL0 = 512 - CT_ASLOTS * 16;
+constexpr int CT_THREADS = 448;  // producer, MMA, 8 epilogue warps, 4 copier warps
 
 __device__ __forceinline__ void ct_item(const CtArgs& a, int item, int& tile, int& g0, int& g1) {
     const int split = item / a.ntiles;  // split-major: concurrent CTAs share one k window in L2
@@ -824,8 +788,10 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * CT_STAGE);
     uint64_t* empty = full + a.stages;
-    uint64_t* tfull = empty + a.stages;  // [2]
-    uint64_t* tempty = tfull + 2;        // [2]
+    uint64_t* afull = empty + a.stages;    // [CT_ASLOTS]
+    uint64_t* aempty = afull + CT_ASLOTS;  // [CT_ASLOTS]
+    uint64_t* tfull = aempty + CT_ASLOTS;  // [2]
+    uint64_t* tempty = tfull + 2;          // [2]
     uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
     const int warp = threadIdx.x / 32;
@@ -834,9 +800,13 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
+        for (int r = 0; r < CT_ASLOTS; ++r) {
+            tc::mbar_init(&afull[r], 128);
+            tc::mbar_init(&aempty[r], 1);
+        }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&tfull[b], 1);
-            tc::mbar_init(&tempty[b], 4);
+            tc::mbar_init(&tempty[b], 8);
         }
         *abort_flag = 0;
         tc::fence_barrier_init();
@@ -849,7 +819,7 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
     const size_t blk = (size_t)MM * MK;  // elements of one slice block
 
     if (threadIdx.x == 0) {
-        // ---- producer
+        // ---- producer: one stage per k block
         int s = 0;
         uint32_t ph = 0;
         long kg = 0;
@@ -862,82 +832,147 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             const __nv_bfloat16* pb = a.Xd + (size_t)(tb.y / 2) * a.nkbt * NSL * blk + (size_t)(tb.y % 2) * (CT_N * MK);
             for (int g = g0; ok && g < g1; ++g) {
                 const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
-                for (int pass = 0; ok && pass < NPASS; ++pass) {
-                    const int na = pass_na(pass), nb = pass_nb(pass);
-                    for (int kb = kb0; kb < kb1; ++kb, ++kg) {
-                        if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
-                            ok = false;
-                            break;
+                for (int kb = kb0; kb < kb1; ++kb, ++kg) {
+                    if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* st = smem + (size_t)s * CT_STAGE;
+                    tc::mbar_arrive_expect_tx(&full[s], (uint32_t)CT_STAGE);
+                    tc::bulk_load(st, pa + (size_t)kb * NSL * blk, (uint32_t)(NSL * BF_SLICE), &full[s]);
+                    for (int t = 0; t < NSL; ++t)
+                        tc::bulk_load(st + CT_OFF_B + t * (CT_N * MK * 2), pb + ((size_t)kb * NSL + t) * blk, CT_N * MK * 2,
+                                      &full[s]);
+                    if (++s == a.stages) {
+                        s = 0;
+                        ph ^= 1u;
+                    }
+                }
+            }
+        }
+    } else if (warp >= 6 && warp < 10) {
+        // ---- copiers: row `row` of each A slice (swizzled BF16 in the stage) into a TMEM slot,
+        // two slices per step
+        const int q = warp % 4;
+        const int row = q * 32 + (threadIdx.x % 32);
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        int s = 0, r = 0;
+        uint32_t ph = 0, pr = 0;
+        long used = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
+            int tile, g0, g1;
+            ct_item(a, item, tile, g0, g1);
+            for (int g = g0; ok && g < g1; ++g) {
+                const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
+                for (int kb = kb0; ok && kb < kb1; ++kb) {
+                    if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint8_t* st = smem + (size_t)s * CT_STAGE;
+#pragma unroll 1
+                    for (int j0 = 0; ok && j0 < NSL; j0 += 2) {
+                        const int nj = NSL - j0 < 2 ? NSL - j0 : 2;
+                        int slot[2] = {0, 0};
+                        for (int jj = 0; jj < nj; ++jj, ++used) {
+                            if (used >= CT_ASLOTS && !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
+                                ok = false;
+                                break;
+                            }
+                            slot[jj] = r;
+                            if (++r == CT_ASLOTS) {
+                                r = 0;
+                                pr ^= 1u;
+                            }
                         }
-                        uint8_t* st = smem + (size_t)s * CT_STAGE;
-                        tc::mbar_arrive_expect_tx(&full[s], (uint32_t)(na * BF_SLICE + nb * CT_N * MK * 2));
-                        tc::bulk_load(st, pa + ((size_t)kb * NSL + pass_a0(pass)) * blk, (uint32_t)(na * BF_SLICE), &full[s]);
-                        for (int t = 0; t < nb; ++t)
-                            tc::bulk_load(st + CT_OFF_B + t * (CT_N * MK * 2), pb + ((size_t)kb * NSL + t) * blk,
-                                          CT_N * MK * 2, &full[s]);
-                        if (++s == a.stages) {
-                            s = 0;
-                            ph ^= 1u;
+                        if (!ok) break;
+                        tc::tc_fence_after();
+                        for (int jj = 0; jj < nj; ++jj) {
+                            const uint8_t* src = st + (j0 + jj) * BF_SLICE;
+                            uint32_t o[16];
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                const uint4 v = *reinterpret_cast<const uint4*>(src + tc::swz_offset((uint32_t)row, (uint32_t)c));
+                                o[4 * c] = v.x;
+                                o[4 * c + 1] = v.y;
+                                o[4 * c + 2] = v.z;
+                                o[4 * c + 3] = v.w;
+                            }
+                            tmem_st16(lane_base + (uint32_t)(CT_ACOL0 + 16 * slot[jj]), o);
                         }
+                        tmem_wait_st();
+                        tc::tc_fence_before();
+                        for (int jj = 0; jj < nj; ++jj) tc::mbar_arrive(&afull[slot[jj]]);
+                    }
+                    if (++s == a.stages) {
+                        s = 0;
+                        ph ^= 1u;
                     }
                 }
             }
         }
     } else if (threadIdx.x == 32) {
-        // ---- MMA issuer: one accumulation run (three passes) per group
-        int s = 0;
-        uint32_t ph = 0;
+        // ---- MMA issuer: per group one accumulation run; per k block seven A slices from TMEM
+        int s = 0, r = 0;
+        uint32_t ph = 0, pr = 0;
         int gi = 0;
         const uint32_t smem_base = tc::smem_u32(smem);
         const uint32_t id = tc::idesc_bf16_f32(MM, CT_N, false);
-        const uint64_t a_step = (uint64_t)(BF_SLICE >> 4), b_step = (uint64_t)((CT_N * MK * 2) >> 4);
+        const uint64_t b_step = (uint64_t)((CT_N * MK * 2) >> 4);
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
             int tile, g0, g1;
             ct_item(a, item, tile, g0, g1);
             for (int g = g0; ok && g < g1; ++g, ++gi) {
-                const int buf = gi % a.nbuf, use = gi / a.nbuf;
-                if (use > 0 && !tc::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), abort_flag, a.err)) {
+                if (gi > 0 && !tc::mbar_wait(&tempty[0], (uint32_t)((gi - 1) & 1), abort_flag, a.err)) {
                     ok = false;
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t d0 = tmem + (uint32_t)(buf * NACC * CT_N);
-                uint32_t d[NACC];
+                uint32_t d[CT_NACC];
 #pragma unroll
-                for (int L = 0; L < NACC; ++L) d[L] = d0 + (uint32_t)(L * CT_N);
+                for (int L = 0; L < CT_NACC; ++L) d[L] = tmem + (uint32_t)(L * CT_N);
                 const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
-                for (int pass = 0; ok && pass < NPASS; ++pass) {
-                    for (int kb = kb0; kb < kb1; ++kb) {
-                        if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                for (int kb = kb0; ok && kb < kb1; ++kb) {
+                    if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint64_t dB = tc::sdesc_kmajor(smem_base + (uint32_t)(s * CT_STAGE + CT_OFF_B));
+                    const bool first = kb == kb0;
+#pragma unroll
+                    for (int j = 0; j < NSL; ++j) {
+                        if (!tc::mbar_wait(&afull[r], pr, abort_flag, a.err)) {
                             ok = false;
                             break;
                         }
                         tc::tc_fence_after();
-                        const uint32_t st = smem_base + (uint32_t)(s * CT_STAGE);
-                        const uint64_t dA = tc::sdesc_kmajor(st), dB = tc::sdesc_kmajor(st + CT_OFF_B);
-#pragma unroll
-                        for (int ks = 0; ks < MK / 16; ++ks) {
-                            const uint64_t ko = (uint64_t)(2 * ks);
-                            issue_pairs(pass, d, dA + ko, dB + ko, a_step, b_step, id,
-                                        (pass | (kb - kb0) | ks) != 0 ? 1u : 0u);
-                        }
-                        tc::mma_commit(&empty[s]);
-                        if (++s == a.stages) {
-                            s = 0;
-                            ph ^= 1u;
+                        issue_slice_j<CT_NACC>(j, d, tmem + (uint32_t)(CT_ACOL0 + 16 * r), dB, b_step, id, first);
+                        tc::mma_commit(&aempty[r]);
+                        if (++r == CT_ASLOTS) {
+                            r = 0;
+                            pr ^= 1u;
                         }
                     }
+                    if (!ok) break;
+                    tc::mma_commit(&empty[s]);
+                    if (++s == a.stages) {
+                        s = 0;
+                        ph ^= 1u;
+                    }
                 }
-                tc::mma_commit(&tfull[buf]);
+                tc::mma_commit(&tfull[0]);
             }
         }
     } else if (warp >= 2) {
-        // ---- epilogue: per group, scale the six accumulators and add them into a
-        // double-float running sum (64 columns per thread); one FP64 partial tile per item
+        // ---- epilogue (warps 2-5 and 10-13, 32 columns each): per group, scale the six
+        // accumulators and add them into a double-float running sum; one FP64 tile per item
         const int q = warp % 4;
+        const int half = warp >= 10 ? 1 : 0;
         const int r = q * 32 + (threadIdx.x % 32);
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        constexpr int HC = CT_N / 2;
         int gi = 0;
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
@@ -945,13 +980,12 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             ct_item(a, item, tile, g0, g1);
             const int2 tb = a.tiles[tile];
             const int m = tb.x * MM + r;
-            const int n0 = tb.y * CT_N;
-            float RH[CT_N], RL[CT_N];
+            const int n0 = tb.y * CT_N + half * HC;
+            float RH[HC], RL[HC];
 #pragma unroll
-            for (int c = 0; c < CT_N; ++c) RH[c] = RL[c] = 0.f;
+            for (int c = 0; c < HC; ++c) RH[c] = RL[c] = 0.f;
             for (int g = g0; g < g1; ++g, ++gi) {
-                const int buf = gi % a.nbuf, use = gi / a.nbuf;
-                ok = tc::mbar_wait(&tfull[buf], (uint32_t)(use & 1), abort_flag, a.err);
+                ok = tc::mbar_wait(&tfull[0], (uint32_t)(gi & 1), abort_flag, a.err);
                 __syncwarp();
                 if (!ok || *abort_flag) {
                     ok = false;
@@ -960,17 +994,18 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                 tc::tc_fence_after();
                 const float rs = a.Sx[(size_t)g * a.nbf_p + m];
                 const float* cs = a.Sx + (size_t)g * a.nbf_p + n0;
-                const uint32_t cb = lane_base + (uint32_t)(buf * NACC * CT_N);
 #pragma unroll
-                for (int c0 = 0; c0 < CT_N; c0 += 8) {
-                    uint32_t v[NACC][8];
+                for (int c0 = 0; c0 < HC; c0 += 4) {
+                    uint32_t v[CT_NACC][4];
 #pragma unroll
-                    for (int L = 0; L < NACC; ++L) tc::tmem_ld8(cb + (uint32_t)(L * CT_N + c0), v[L]);
+                    for (int L = 0; L < CT_NACC; ++L)
+                        tc::tmem_ld4_nowait(lane_base + (uint32_t)(L * CT_N + half * HC + c0), v[L]);
+                    tc::tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        float acc[NACC];
+                    for (int j = 0; j < 4; ++j) {
+                        float acc[CT_NACC];
 #pragma unroll
-                        for (int L = 0; L < NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
+                        for (int L = 0; L < CT_NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
                         float hi, lo;
                         combine6(acc, hi, lo);
                         const float sc = rs * cs[c0 + j];
@@ -979,12 +1014,12 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                 }
                 tc::tc_fence_before();
                 __syncwarp();
-                if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[buf]);
+                if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[0]);
             }
             if (!ok) break;
-            double* dst = a.part + (((size_t)(item / a.ntiles) * a.ntiles + tile) * MM + r) * CT_N;
+            double* dst = a.part + (((size_t)(item / a.ntiles) * a.ntiles + tile) * MM + r) * CT_N + half * HC;
 #pragma unroll
-            for (int c = 0; c < CT_N; c += 2)
+            for (int c = 0; c < HC; c += 2)
                 *reinterpret_cast<double2*>(dst + c) =
                     make_double2((double)RH[c] + (double)RL[c], (double)RH[c + 1] + (double)RL[c + 1]);
         }
@@ -1291,7 +1326,6 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         ca.nkbt = nkbt;
         ca.part = o->part;
         ca.stages = ct_stages;
-        ca.nbuf = 1;
         ca.n_items = o->ntiles * nsplit;
         ca.err = o->err;
         oz_contract_kernel<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
