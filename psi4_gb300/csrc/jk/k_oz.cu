@@ -350,7 +350,7 @@ struct TrArgs {
 // Its accumulators: levels 0-3 exact and a tail (4-6); the round-toward-zero truncation of
 // the tail is harmless here (no sums of squares; it is random relative to X).
 constexpr int TR_NACC = 5;
-constexpr int TR_ASLOTS = 4;
+constexpr int TR_ASLOTS = 7;  // a whole k block of A slices: the converters run one k block ahead
 constexpr int TR_ACOL0 = 512 - TR_ASLOTS * 16;  // first A-slot column
 constexpr int TR_OFF_C = NSL * I8_SLICE;        // stage: [7 int8 A slices | 7 BF16 C^T slices]
 
@@ -766,11 +766,11 @@ struct CtArgs {
 
 // Stage per k block: [7 A slices, 128 rows | 7 B slices, 64 rows].  The copier warps move each
 // A slice into a TMEM slot (the MMAs take A from tensor memory and only B from shared memory);
-// six accumulators (levels 0-4 exact, tail 5-6) at TMEM columns 0..383, A slots at 448..511.
+// six accumulators (levels 0-4 exact, tail 5-6) at TMEM columns 0..383, A slots at 400..511.
 constexpr int CT_NACC = NACC;
 constexpr int CT_OFF_B = NSL * BF_SLICE;                  // 56 KB
 constexpr int CT_STAGE = CT_OFF_B + NSL * CT_N * MK * 2;  // + 28 KB
-constexpr int CT_ASLOTS = 4;
+constexpr int CT_ASLOTS = 7;
 constexpr int CT_ACOL0 = 512 - CT_ASLOTS * 16;
 constexpr int CT_THREADS = 448;  // producer, MMA, 8 epilogue warps, 4 copier warps
 

@@ -52,12 +52,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait that may suspend the thread until the phase completes, for at most `ns`
+// nanoseconds, instead of returning at once: a waiting warp then stops issuing instructions
+// and leaves the issue slots of its sub-partition to the warps that work.
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t parity, uint32_t ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait on phase `parity` of `bar`; gives up when the block aborted or on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err) {
     if (mbar_try_wait(bar, parity)) return true;
     uint64_t t0 = global_timer();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait_suspend(bar, parity, 100000u)) return true;
         if (*abort_flag) return false;
         if (global_timer() - t0 > WAIT_NS) {
             *abort_flag = 1;
