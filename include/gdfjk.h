@@ -71,6 +71,16 @@ int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_sk
 /* Same with B already on the device (Q-major packed lower triangle, naux*nbf(nbf+1)/2). */
 int gdfjk_upload_B_device(gdfjk_t h, const double* B_qtri_device);
 
+/* Upload B in blocks of aux functions, the way DFHelper builds it block by block
+ * (DFHelper::prepare_AO_core -> compute_sparse_pQq_blocking_p over Q-shell blocks,
+ * dfhelper.cc:514-588): rows q0 .. q0+nq-1 of the Q-major packed lower triangle
+ * (nq * nbf(nbf+1)/2 doubles; screened pairs must be zero, as DFHelper's sparse tensor
+ * holds no entry for them).
+ * Blocks go in order of q0 starting at 0; the engine is ready for compute once the block
+ * that ends at naux has been uploaded.  Neither call keeps the pointer. */
+int gdfjk_upload_B_block(gdfjk_t h, const double* B_qtri_rows, int q0, int nq);
+int gdfjk_upload_B_device_block(gdfjk_t h, const double* B_qtri_rows_device, int q0, int nq);
+
 /* One Fock build, host buffers (JK::compute, jk.cc:595-681, for one density):
  *   C_left  nbf x nocc (row-major, leading dimension ldc >= nocc)
  *   C_right nbf x nocc or NULL (NULL = lr-symmetric: D = C_left C_left^T, jk.cc:597-599)

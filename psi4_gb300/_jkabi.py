@@ -11,6 +11,8 @@ SIGNATURES = {
     "gdfjk_create": (I, [I, I, I, P, I, ctypes.POINTER(P)]),
     "gdfjk_upload_B": (I, [P, P, I, P, P, P]),
     "gdfjk_upload_B_device": (I, [P, P]),
+    "gdfjk_upload_B_block": (I, [P, P, I, I]),
+    "gdfjk_upload_B_device_block": (I, [P, P, I, I]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_incremental": (I, [P, P, I, I, P, I, I, I, I, P, P]),

@@ -54,6 +54,8 @@ struct gdfjk_s {
     size_t dCin_elems = 0;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float t_j = 0, t_kt = 0, t_kc = 0;
+    bool last_emulated = false;  // the last K went through the emulated-FP64 path
+    int next_q = 0;              // next aux row expected by the block upload
     MixedState* mixed = nullptr;
     OzState* oz = nullptr;
     // backward workspaces
@@ -148,6 +150,7 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
     const bool do_K = mode & GDFJK_DO_K;
     const bool nonsym = C_right != nullptr;
     const int nocc_pad = round_up(std::max(nocc, 0), 32);
+    if (mode & GDFJK_DO_K) h->last_emulated = false;
     int rc = ensure_workspace(h, nocc_pad, nonsym);
     if (rc) return rc;
     cudaStream_t s = h->stream;
@@ -185,6 +188,7 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
             if (rc) return rc;
         } else if (mode & GDFJK_EMULATED) {
             if (nonsym) return set_err(h, GDFJK_ERR_ARG, "emulated-FP64 K needs an lr-symmetric density");
+            h->last_emulated = true;
             rc = oz_build_K(h->oz, h->B, L, h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
             if (rc == GDFJK_ERR_OOM) {  // give the mixed form's split copy of B back and retry once
                 CK(cudaStreamSynchronize(s));
@@ -369,6 +373,62 @@ int gdfjk_destroy(gdfjk_t h) {
 }
 
 void* gdfjk_stream(gdfjk_t h) { return h ? (void*)h->stream : nullptr; }
+
+// Rows [q0, q0 + nq) of the packed triangle, device pointer, into the stored tiles.
+static int upload_rows_device(gdfjk_t h, const double* Bq, int q0, int nq) {
+    int rc;
+    if (q0 == 0) {
+        if (!h->B) {
+            if ((rc = dalloc(h, &h->B, (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+        }
+        h->B_ready = false;
+        mixed_invalidate(h->mixed);
+        oz_invalidate(h->oz);
+        h->next_q = 0;
+    }
+    if (q0 != h->next_q) return set_err(h, GDFJK_ERR_STATE, "upload_B_block: blocks must follow each other from q0 = 0");
+    TileLayout L = layout_of(h);
+    launch_relayout_qtri(Bq, q0, nq, h->nbf, L, h->B, h->stream);
+    CK(cudaGetLastError());
+    if ((rc = wait_stream(h, env_timeout()))) return rc;
+    h->next_q = q0 + nq;
+    if (h->next_q == h->naux) h->B_ready = true;
+    return GDFJK_OK;
+}
+
+int gdfjk_upload_B_device_block(gdfjk_t h, const double* Bq, int q0, int nq) {
+    if (!h || !Bq) return set_err(h, GDFJK_ERR_ARG, "upload_B_device_block: null argument");
+    if (q0 < 0 || nq <= 0 || q0 + nq > h->naux) return set_err(h, GDFJK_ERR_ARG, "upload_B_device_block: bad q0 / nq");
+    CK(cudaSetDevice(h->device));
+    return upload_rows_device(h, Bq, q0, nq);
+}
+
+int gdfjk_upload_B_block(gdfjk_t h, const double* Bq, int q0, int nq) {
+    if (!h || !Bq) return set_err(h, GDFJK_ERR_ARG, "upload_B_block: null argument");
+    if (q0 < 0 || nq <= 0 || q0 + nq > h->naux) return set_err(h, GDFJK_ERR_ARG, "upload_B_block: bad q0 / nq");
+    CK(cudaSetDevice(h->device));
+    const size_t npair = (size_t)h->nbf * (h->nbf + 1) / 2;
+    // staged through the host-path buffer in sub-blocks of at most 512 MB
+    const int sub = (int)std::max<size_t>(1, std::min<size_t>((size_t)nq, (size_t)(512u << 20) / (npair * 8)));
+    double* stage = nullptr;
+    if (cudaMalloc(&stage, (size_t)sub * npair * 8) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(h, GDFJK_ERR_OOM, "upload_B_block: staging buffer refused");
+    }
+    int rc = GDFJK_OK;
+    for (int k = 0; k < nq && rc == GDFJK_OK; k += sub) {
+        const int n = std::min(sub, nq - k);
+        if (cudaMemcpyAsync(stage, Bq + (size_t)k * npair, (size_t)n * npair * 8, cudaMemcpyHostToDevice, h->stream) !=
+            cudaSuccess) {
+            rc = set_err(h, GDFJK_ERR_CUDA, "upload_B_block: host-to-device copy failed");
+            break;
+        }
+        rc = upload_rows_device(h, stage, q0 + k, n);
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaFree(stage);
+    return rc;
+}
 
 int gdfjk_upload_B_device(gdfjk_t h, const double* Bq) {
     if (!h || !Bq) return set_err(h, GDFJK_ERR_ARG, "upload_B_device: null argument");
@@ -685,6 +745,13 @@ int gdfjk_last_timings(gdfjk_t h, double* j_ms, double* kt_ms, double* kc_ms) {
     CK(cudaEventElapsedTime(&a, h->ev[0], h->ev[1]));
     CK(cudaEventElapsedTime(&b, h->ev[2], h->ev[3]));
     CK(cudaEventElapsedTime(&c, h->ev[3], h->ev[4]));
+    if (h->last_emulated) {
+        // batches interleave transform and contraction: report the transform kernels' own time
+        // and the rest of K (digits of C, splits, contractions, reductions) as the contraction
+        const float k_all = b + c;
+        b = oz_last_transform_ms(h->oz);
+        c = k_all - b;
+    }
     if (j_ms) *j_ms = a;
     if (kt_ms) *kt_ms = b;
     if (kc_ms) *kc_ms = c;

@@ -1082,9 +1082,21 @@ struct OzState {
     int* err = nullptr;
     int num_sms = 0;
     bool attrs_set = false;
+    std::vector<cudaEvent_t> tr_ev;  // begin/end of each batch's half-transform, last build
+    int n_tr = 0;
 };
 
 OzState* oz_create() { return new OzState(); }
+
+float oz_last_transform_ms(OzState* o) {
+    if (!o) return 0.f;
+    float total = 0.f;
+    for (int b = 0; b < o->n_tr; ++b) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, o->tr_ev[2 * b], o->tr_ev[2 * b + 1]) == cudaSuccess) total += ms;
+    }
+    return total;
+}
 
 namespace {
 
@@ -1140,6 +1152,7 @@ void oz_destroy(OzState* o) {
     void* ps[] = {o->eC, o->sC, o->Cd, o->xmax, o->Sx, o->part, o->d_tiles, o->d_tob, o->err};
     for (void* p : ps)
         if (p) cudaFree(p);
+    for (cudaEvent_t e : o->tr_ev) cudaEventDestroy(e);
     delete o;
 }
 
@@ -1265,6 +1278,16 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         err = "emulated FP64: pipeline stages do not fit in shared memory";
         return GDFJK_ERR_ARG;
     }
+    const int nbatch = (naux + qb - 1) / qb;
+    while ((int)o->tr_ev.size() < 2 * nbatch) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            err = "emulated FP64: cudaEventCreate failed";
+            return GDFJK_ERR_CUDA;
+        }
+        o->tr_ev.push_back(e);
+    }
+    o->n_tr = nbatch;
     for (int q0 = 0, batch = 0; q0 < naux; q0 += qb, ++batch) {
         const int nq = std::min(qb, naux - q0);
         const int ngroups = (nq + G - 1) / G;
@@ -1297,7 +1320,9 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;
         ta.n_items = nq * nmb * nchunk;
         ta.err = o->err;
+        cudaEventRecord(o->tr_ev[2 * batch], s);
         oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
+        cudaEventRecord(o->tr_ev[2 * batch + 1], s);
         // the transform phase ends with the last batch's half-transform kernel
         if (ev_transform_done && q0 + qb >= naux) cudaEventRecord(ev_transform_done, s);
         oz_split_X_kernel<<<dim3((unsigned)nmb, (unsigned)ngroups), 256, 0, s>>>(

@@ -21,6 +21,9 @@ size_t oz_query_memory(int nbf, int naux, int max_nocc);
 // row-major); records `ev_transform_done` after the last half-transform.
 int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int naux, const double* Cpad, int nocc,
                int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err);
+// Summed device time (ms) of the half-transform kernels of the last build (all batches);
+// valid once that build has completed.
+float oz_last_transform_ms(OzState* o);
 // error bits raised by the tensor-core kernels since the last call (0 = none); clears them
 int oz_error_flag(OzState* o, cudaStream_t s);
 

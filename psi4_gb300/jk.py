@@ -73,6 +73,16 @@ class DFJKEngine:
         """B already in device memory as the Q-major packed triangle (e.g. a torch tensor)."""
         self._check(self.L.gdfjk_upload_B_device(self.h, ctypes.c_void_p(ptr)))
 
+    def upload_block(self, rows: np.ndarray, q0: int):
+        """Rows q0 .. q0+len(rows)-1 of the Q-major packed triangle from host memory; blocks in
+        order from q0 = 0, ready once the last row has been uploaded."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        self._check(self.L.gdfjk_upload_B_block(self.h, _p(rows), int(q0), int(rows.shape[0])))
+
+    def upload_device_block(self, ptr: int, q0: int, nq: int):
+        """Rows q0 .. q0+nq-1 of the packed triangle already in device memory."""
+        self._check(self.L.gdfjk_upload_B_device_block(self.h, ctypes.c_void_p(ptr), int(q0), int(nq)))
+
     # ---- builds
     def compute(self, C_left, C_right=None, mode=abi.DO_J | abi.DO_K, want_D=False):
         Cl = np.ascontiguousarray(C_left, dtype=np.float64)
