@@ -294,8 +294,13 @@ def run_gpu(args):
         issued = oz_issued_flops(nbf, naux, nocc)
         bf16_sus = float(peaks.get("bf16_tflops_sustained", 1696.1))
         bf16_burst = float(peaks.get("bf16_tflops", 1885.4))
+        # DRAM bytes of oz_transform_kernel from an ncu capture at naux 128 (3.72 GB per launch,
+        # profiles/oz_kernels_ncu.md), scaled by the aux functions processed
+        traffic = 3.72e9 * naux / 128.0 if (nbf, nocc) == (1856, 160) else None
         roofline = {"bound": "tensor", "kernel": "oz_transform_kernel", "achieved": issued / kt / 1e12,
-                    "peak": bf16_sus, "unit": "TFLOP/s", "frac": issued / kt / 1e12 / bf16_sus, "traffic": None,
+                    "peak": bf16_sus, "unit": "TFLOP/s", "frac": issued / kt / 1e12 / bf16_sus, "traffic": traffic,
+                    "traffic_note": "DRAM bytes per build, scaled from an ncu capture of the same kernel at naux 128 "
+                                    "(its algorithmic bytes: int8 digits of B 7*naux*nbf_p^2 + X 8*nbf*naux*nocc_p)",
                     "frac_of_burst": issued / kt / 1e12 / bf16_burst,
                     "peak_source": "bf16_tflops_sustained of measured (MEASURED_PEAKS.json): the kernel runs inside "
                                    "back-to-back builds",
