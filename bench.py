@@ -561,25 +561,41 @@ def measure_screened(cfg, dev, args, peaks):
     J = torch.empty((nbf, nbf), dtype=torch.float64, device=dev)
     K = torch.empty_like(J)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    def timed(mode, n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            eng.compute_device(C.data_ptr(), None, nocc, nocc, mode, None, J.data_ptr(), K.data_ptr())
+        e1.record(stream)
+        eng.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / n, eng.timings()
+
+    emulated = None
+    try:
+        # the emulated form first (its digit copy of B is block-sparse), then released
+        em = abi.DO_J | abi.DO_K | abi.EMULATED
+        timed(em, 1)
+        te, tme = timed(em, 2)
+        emulated = {"builds_per_s": 1.0 / te, "ms_per_build": 1e3 * te, "phase_ms": tme}
+        eng.trim()
+    except Exception as ex:
+        emulated = {"unavailable": str(ex)[:300]}
     mode = abi.DO_J | abi.DO_K
-    eng.compute_device(C.data_ptr(), None, nocc, nocc, mode, None, J.data_ptr(), K.data_ptr())
-    eng.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    eng.compute_device(C.data_ptr(), None, nocc, nocc, mode, None, J.data_ptr(), K.data_ptr())
-    e1.record(stream)
-    eng.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
-    tm = eng.timings()
+    timed(mode, 1)
+    t, tm = timed(mode, 1)
     s_sq = int(sp.pair_mask.sum())
     out = {"workload": desc + " (Schwarz mask from the real integrals, synthetic B on significant pairs)",
            "nbf": nbf, "naux": naux, "nocc": nocc, "pair_fraction": s_sq / float(nbf * nbf),
            "mask_seconds": t_mask,
            "fp64": {"builds_per_s": 1.0 / t, "ms_per_build": 1e3 * t, "phase_ms": tm,
                     "k_flops_algorithmic": 2.0 * naux * s_sq * nocc + float(nbf) * (nbf + 1) * naux * nocc},
-           "tensor_core_forms": "unavailable at this size: their dense digit/split copies of B would need "
-                                f"{naux * (-(-nbf // 128) * 128) ** 2 * 7 / 1e9:.0f} GB (block-sparse copies are not built)"}
+           "fp64_emulated": emulated,
+           "mixed": "unavailable at this size: its dense split-BF16 copy of B would need "
+                    f"{naux * (-(-nbf // 128) * 128) ** 2 * 4 / 1e9:.0f} GB (a block-sparse copy is built for the "
+                    "emulated form only)"}
+    if emulated and "builds_per_s" in emulated:
+        out["fp64_emulated"]["speedup_vs_native_fp64"] = emulated["builds_per_s"] * t
     eng.close()
     return out
 

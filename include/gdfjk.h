@@ -116,6 +116,12 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
 int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* gJ, const double* gK, double* dC,
                    double* Gamma, int on_device);
 
+/* Release the derived copies of B that the tensor-core forms keep (split BF16 slices, int8
+ * digits) and their X buffers; they are rebuilt on the next build that needs them.  No
+ * counterpart in the reference (psi4's JK keeps no such copies): for callers that need the
+ * device memory back between phases. */
+int gdfjk_trim(gdfjk_t h);
+
 /* Device bytes the engine needs for these sizes (feeds JK::memory_estimate, jk.h:398). */
 int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes);
 

@@ -13,6 +13,7 @@ SIGNATURES = {
     "gdfjk_upload_B_device": (I, [P, P]),
     "gdfjk_upload_B_block": (I, [P, P, I, I]),
     "gdfjk_upload_B_device_block": (I, [P, P, I, I]),
+    "gdfjk_trim": (I, [P]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_incremental": (I, [P, P, I, I, P, I, I, I, I, P, P]),

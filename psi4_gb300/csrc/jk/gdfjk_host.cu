@@ -54,6 +54,7 @@ struct gdfjk_s {
     size_t dCin_elems = 0;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float t_j = 0, t_kt = 0, t_kc = 0;
+    int cap_x = 0;               // nocc_pad the FP64 X buffers hold
     bool last_emulated = false;  // the last K went through the emulated-FP64 path
     int next_q = 0;              // next aux row expected by the block upload
     MixedState* mixed = nullptr;
@@ -105,7 +106,9 @@ int dalloc(gdfjk_t h, T** p, size_t n) {
 
 TileLayout layout_of(gdfjk_t h) { return TileLayout{h->nT, h->ntiles, h->d_tI, h->d_tJ, h->d_map}; }
 
-int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym) {
+// D/J work buffers and the padded C always; the FP64 X buffers and split-K partials only when
+// `need_x` (the native FP64 K and the backward pass use them; the tensor-core forms do not).
+int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym, bool need_x) {
     int rc;
     size_t np2 = (size_t)h->nbf_pad * h->nbf_pad;
     if (!h->D) {
@@ -116,16 +119,20 @@ int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym) {
         int nout_full = h->nT * h->nT;
         if ((rc = dalloc(h, &h->Kt, (size_t)nout_full * TILE_ELEMS))) return rc;
     }
-    if (nocc_pad > h->cap_nocc || (nonsym && !h->Xr && nocc_pad > 0)) {
-        int cap = std::max(nocc_pad, h->cap_nocc);
+    if (nocc_pad > h->cap_nocc) {
+        if ((rc = dalloc(h, &h->Cl, (size_t)h->nbf_pad * std::max(nocc_pad, 1)))) return rc;
+        if ((rc = dalloc(h, &h->Cr, (size_t)h->nbf_pad * std::max(nocc_pad, 1)))) return rc;
+        h->cap_nocc = nocc_pad;
+    }
+    if (!need_x) return GDFJK_OK;
+    if (nocc_pad > h->cap_x || (nonsym && !h->Xr && nocc_pad > 0)) {
+        int cap = std::max(nocc_pad, h->cap_x);
         size_t xe = (size_t)h->nbf_pad * h->naux * cap;
-        if ((rc = dalloc(h, &h->Cl, (size_t)h->nbf_pad * std::max(cap, 1)))) return rc;
-        if ((rc = dalloc(h, &h->Cr, (size_t)h->nbf_pad * std::max(cap, 1)))) return rc;
         if ((rc = dalloc(h, &h->Xl, xe))) return rc;
         if (nonsym || h->Xr) {
             if ((rc = dalloc(h, &h->Xr, xe))) return rc;
         }
-        h->cap_nocc = cap;
+        h->cap_x = cap;
     }
     // split-K partials
     size_t kdim = (size_t)h->naux * std::max(nocc_pad, 1);
@@ -151,7 +158,8 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
     const bool nonsym = C_right != nullptr;
     const int nocc_pad = round_up(std::max(nocc, 0), 32);
     if (mode & GDFJK_DO_K) h->last_emulated = false;
-    int rc = ensure_workspace(h, nocc_pad, nonsym);
+    const bool native_k = do_K && nocc > 0 && !(mode & GDFJK_MIXED) && !(mode & GDFJK_EMULATED);
+    int rc = ensure_workspace(h, nocc_pad, nonsym, native_k);
     if (rc) return rc;
     cudaStream_t s = h->stream;
     TileLayout L = layout_of(h);
@@ -189,11 +197,11 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
         } else if (mode & GDFJK_EMULATED) {
             if (nonsym) return set_err(h, GDFJK_ERR_ARG, "emulated-FP64 K needs an lr-symmetric density");
             h->last_emulated = true;
-            rc = oz_build_K(h->oz, h->B, L, h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
+            rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
             if (rc == GDFJK_ERR_OOM) {  // give the mixed form's split copy of B back and retry once
                 CK(cudaStreamSynchronize(s));
                 mixed_invalidate(h->mixed);
-                rc = oz_build_K(h->oz, h->B, L, h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
+                rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
             }
             if (rc) return rc;
         } else {
@@ -657,7 +665,7 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
     cudaStream_t s = h->stream;
     const int nbf = h->nbf, nbf_pad = h->nbf_pad, naux = h->naux;
     const int nocc_pad = round_up(std::max(nocc, 0), 32);
-    int rc = ensure_workspace(h, std::max(nocc_pad, 32), false);
+    int rc = ensure_workspace(h, std::max(nocc_pad, 32), false, true);
     if (rc) return rc;
     size_t np2 = (size_t)nbf_pad * nbf_pad, n2 = (size_t)nbf * nbf;
     size_t npair = (size_t)nbf * (nbf + 1) / 2;
@@ -735,6 +743,16 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
         if ((rc = wait_stream(h, env_timeout()))) return rc;
         return check_device_flag(h);
     }
+    return GDFJK_OK;
+}
+
+int gdfjk_trim(gdfjk_t h) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "trim: null handle");
+    CK(cudaSetDevice(h->device));
+    int rc = wait_stream(h, env_timeout());
+    if (rc) return rc;
+    mixed_invalidate(h->mixed);
+    oz_release(h->oz);
     return GDFJK_OK;
 }
 

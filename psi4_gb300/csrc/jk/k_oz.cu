@@ -177,19 +177,21 @@ __global__ void oz_rowmax_kernel(const double* __restrict__ B, int ntiles, const
     }
 }
 
-// Int8 digit fields of B, one 24 KB block per (Q, 128-row block, 32-wide k block):
-// [slice 6][row 128][k 32] of (d_s + 64).  Block (Q, mb, kb) = blockIdx.x; 256 threads.
+// Int8 digit fields of B, one 28 KB block per (Q, listed (128-row block, 32-wide k block)):
+// [slice 7][row 128][k 32] of (d_s + 64).  blockIdx.x = Q * nnz + b; 256 threads.  Only the
+// blocks that touch a stored tile are listed (blk_mb/blk_kb, grouped by row block).
 // The 128 x 32 FP64 window is staged in shared memory from the stored tiles (lower tiles
 // row-wise, upper ones through their stored mirror column-wise, both coalesced).
 __global__ void __launch_bounds__(256) oz_split_B_kernel(const double* __restrict__ B, int nbf, int nT, int ntiles,
-                                                         const int* __restrict__ map, int nbf_p,
+                                                         const int* __restrict__ map, int nbf_p, int nnz,
+                                                         const int* __restrict__ blk_mb, const int* __restrict__ blk_kb,
+                                                         const int* __restrict__ mb_ptr,
                                                          const unsigned long long* __restrict__ rowmax,
                                                          float* __restrict__ sA, uint8_t* __restrict__ Bd) {
-    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
     const size_t id = blockIdx.x;
-    const int kb = (int)(id % nkb);
-    const int mb = (int)((id / nkb) % nmb);
-    const int Q = (int)(id / ((size_t)nkb * nmb));
+    const int b = (int)(id % nnz);
+    const int Q = (int)(id / nnz);
+    const int mb = blk_mb[b], kb = blk_kb[b];
     __shared__ double win[MM][MK + 1];
     __shared__ int Es[MM];
     const int J = (kb * MK) / TILE, c0 = (kb * MK) % TILE;
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(256) oz_split_B_kernel(const double* __restric
         const int m = mb * MM + threadIdx.x;
         const int E = exp_of_max_d(rowmax[(size_t)Q * nbf_p + m]);
         Es[threadIdx.x] = E;
-        if (kb == 0) sA[(size_t)Q * nbf_p + m] = scale_of(E);
+        if (b == mb_ptr[mb]) sA[(size_t)Q * nbf_p + m] = scale_of(E);
     }
     __syncthreads();
     uint8_t* out = Bd + id * I8_BLOCK;
@@ -338,7 +340,10 @@ struct TrArgs {
     float2* Xdf;               // [nbf][kdim_b] X as (hi, lo), k = (Q - q0) * nocc_p + i
     unsigned* xmax;            // [nbf][ngroups] max |hi| per (row, group of G aux functions)
     int q0, nq, nmb, nkb, nbf, nbf_p, nocc_p, N, nchunk, G, ngroups;
-    int run_kb, nrun;          // k blocks per accumulation run, runs per item
+    const int* mb_ptr;         // listed k blocks of row block mb: mb_kb[mb_ptr[mb] .. mb_ptr[mb+1])
+    const int* mb_kb;
+    int nnz;                   // listed blocks in all (the digit blocks of one Q)
+    int run_kb;                // listed k blocks per accumulation run, at most
     size_t kdim_b;
     int stages, nbuf, n_items, ncols;
     int* err;
@@ -360,9 +365,12 @@ __device__ __forceinline__ void tr_item(const TrArgs& a, int item, int& Q, int& 
     mb = rest % a.nmb;
     Q = a.q0 + rest / a.nmb;
 }
-__device__ __forceinline__ void tr_run(const TrArgs& a, int run, int& kb0, int& kb1) {
-    kb0 = run * a.run_kb;
-    kb1 = min(a.nkb, kb0 + a.run_kb);
+// the listed k blocks of row block mb: first list position, count, runs, positions per run
+__device__ __forceinline__ void tr_blocks(const TrArgs& a, int mb, int& p0, int& cnt, int& nrun, int& rlen) {
+    p0 = a.mb_ptr[mb];
+    cnt = a.mb_ptr[mb + 1] - p0;
+    nrun = max(1, (cnt + a.run_kb - 1) / a.run_kb);
+    rlen = (cnt + nrun - 1) / nrun;
 }
 
 // a[0] + ... + a[4]: four exact level sums and the tail, as an FP32 pair
@@ -480,17 +488,19 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
         for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
             int Q, mb, chunk;
             tr_item(a, item, Q, mb, chunk);
-            const uint8_t* pa = a.Bd + ((size_t)Q * a.nmb + mb) * a.nkb * I8_BLOCK;
+            int p0, cnt, nrun, rlen;
+            tr_blocks(a, mb, p0, cnt, nrun, rlen);
+            const uint8_t* pa = a.Bd + ((size_t)Q * a.nnz + p0) * I8_BLOCK;
             const __nv_bfloat16* pc = a.Cd + (size_t)chunk * a.nkb * NSL * N * MK;
-            for (int kb = 0; kb < a.nkb; ++kb, ++kg) {
+            for (int p = 0; p < cnt; ++p, ++kg) {
                 if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
                     ok = false;
                     break;
                 }
                 uint8_t* st = smem + (size_t)s * stage_bytes;
                 tc::mbar_arrive_expect_tx(&full[s], (uint32_t)I8_BLOCK + cbytes);
-                tc::bulk_load(st, pa + (size_t)kb * I8_BLOCK, (uint32_t)I8_BLOCK, &full[s]);
-                tc::bulk_load(st + TR_OFF_C, pc + (size_t)kb * NSL * N * MK, cbytes, &full[s]);
+                tc::bulk_load(st, pa + (size_t)p * I8_BLOCK, (uint32_t)I8_BLOCK, &full[s]);
+                tc::bulk_load(st + TR_OFF_C, pc + (size_t)a.mb_kb[p0 + p] * NSL * N * MK, cbytes, &full[s]);
                 if (++s == a.stages) {
                     s = 0;
                     ph ^= 1u;
@@ -508,7 +518,10 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
         long used = 0;
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
-            for (int kb = 0; ok && kb < a.nkb; ++kb) {
+            int Q, mb, chunk, p0, cnt, nrun, rlen;
+            tr_item(a, item, Q, mb, chunk);
+            tr_blocks(a, mb, p0, cnt, nrun, rlen);
+            for (int p = 0; ok && p < cnt; ++p) {
                 if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
                     ok = false;
                     break;
@@ -572,7 +585,10 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
         const uint64_t b_step = (uint64_t)(c_slice >> 4);
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.n_items && !*abort_flag; item += gridDim.x) {
-            for (int run = 0; ok && run < a.nrun; ++run, ++ri) {
+            int Q, mb, chunk, p0, cnt, nrun, rlen;
+            tr_item(a, item, Q, mb, chunk);
+            tr_blocks(a, mb, p0, cnt, nrun, rlen);
+            for (int run = 0; ok && run < nrun; ++run, ++ri) {
                 const int buf = ri % a.nbuf, use = ri / a.nbuf;
                 if (use > 0 && !tc::mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), abort_flag, a.err)) {
                     ok = false;
@@ -583,8 +599,7 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                 uint32_t d[TR_NACC];
 #pragma unroll
                 for (int L = 0; L < TR_NACC; ++L) d[L] = d0 + (uint32_t)(L * N);
-                int kb0, kb1;
-                tr_run(a, run, kb0, kb1);
+                const int kb0 = run * rlen, kb1 = min(cnt, kb0 + rlen);  // list positions of this run
                 for (int kb = kb0; ok && kb < kb1; ++kb) {
                     if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
                         ok = false;
@@ -634,7 +649,9 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
             const float sa = valid ? a.sA[(size_t)Q * a.nbf_p + m] : 0.f;
             float2* xrow = a.Xdf + (valid ? (size_t)m * a.kdim_b + (size_t)(Q - a.q0) * a.nocc_p : 0);
             float rmax = 0.f;
-            for (int run = 0; run < a.nrun; ++run, ++ri) {
+            int p0, cnt, nrun, rlen;
+            tr_blocks(a, mb, p0, cnt, nrun, rlen);
+            for (int run = 0; run < nrun; ++run, ++ri) {
                 const int buf = ri % a.nbuf, use = ri / a.nbuf;
                 ok = tc::mbar_wait(&tfull[buf], (uint32_t)(use & 1), abort_flag, a.err);
                 __syncwarp();
@@ -644,7 +661,7 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                 }
                 tc::tc_fence_after();
                 const uint32_t cb = lane_base + (uint32_t)(buf * TR_NACC * N);
-                const bool last = run == a.nrun - 1;
+                const bool last = run == nrun - 1;
                 for (int c0 = half * (N / 2); c0 < (half + 1) * (N / 2); c0 += 8) {
                     const int i0 = chunk * N + c0;
                     float2 prev[8];
@@ -1084,6 +1101,11 @@ struct OzState {
     bool attrs_set = false;
     std::vector<cudaEvent_t> tr_ev;  // begin/end of each batch's half-transform, last build
     int n_tr = 0;
+    // (128-row block, 32-wide k block) pairs of B that touch a stored tile, grouped by row block
+    int* d_mb_ptr = nullptr;
+    int* d_mb_kb = nullptr;
+    int* d_blk_mb = nullptr;
+    int nnz = 0, lists_nbf_p = 0;
 };
 
 OzState* oz_create() { return new OzState(); }
@@ -1149,7 +1171,8 @@ void oz_invalidate(OzState* o) {
 void oz_destroy(OzState* o) {
     if (!o) return;
     oz_release(o);
-    void* ps[] = {o->eC, o->sC, o->Cd, o->xmax, o->Sx, o->part, o->d_tiles, o->d_tob, o->err};
+    void* ps[] = {o->eC, o->sC, o->Cd, o->xmax, o->Sx, o->part, o->d_tiles, o->d_tob, o->err, o->d_mb_ptr, o->d_mb_kb,
+                  o->d_blk_mb};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (cudaEvent_t e : o->tr_ev) cudaEventDestroy(e);
@@ -1175,8 +1198,8 @@ int oz_error_flag(OzState* o, cudaStream_t s) {
     return f;
 }
 
-int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int naux, const double* Cpad, int nocc,
-               int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err) {
+int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
+               int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err) {
     using namespace oz;
     int rc;
     const int nbf_p = round_up(nbf, MM);
@@ -1196,17 +1219,48 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         cudaFuncSetAttribute(oz_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
         o->attrs_set = true;
     }
-    // ---- digits of B (once per upload)
+    // ---- the (row block, k block) pairs of B that touch a stored tile (the tile map is fixed)
+    if (o->lists_nbf_p != nbf_p) {
+        std::vector<int> ptr(nmb + 1, 0), kbs, bmb;
+        for (int mb = 0; mb < nmb; ++mb) {
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int J = (kb * MK) / TILE;
+                bool any = false;
+                for (int I = 2 * mb; I <= 2 * mb + 1 && !any; ++I)
+                    if (I < L.nT && J < L.nT) any = map_host[(I >= J ? I : J) * L.nT + (I >= J ? J : I)] >= 0;
+                if (any) {
+                    kbs.push_back(kb);
+                    bmb.push_back(mb);
+                }
+            }
+            ptr[mb + 1] = (int)kbs.size();
+        }
+        if (kbs.empty()) {
+            err = "emulated FP64: B has no stored tiles";
+            return GDFJK_ERR_ARG;
+        }
+        if ((rc = oz_alloc((void**)&o->d_mb_ptr, ptr.size() * sizeof(int), err)) ||
+            (rc = oz_alloc((void**)&o->d_mb_kb, kbs.size() * sizeof(int), err)) ||
+            (rc = oz_alloc((void**)&o->d_blk_mb, bmb.size() * sizeof(int), err)))
+            return rc;
+        cudaMemcpy(o->d_mb_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(o->d_mb_kb, kbs.data(), kbs.size() * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(o->d_blk_mb, bmb.data(), bmb.size() * sizeof(int), cudaMemcpyHostToDevice);
+        o->nnz = (int)kbs.size();
+        o->lists_nbf_p = nbf_p;
+        o->B_ready = false;
+    }
+    // ---- digits of B (once per upload), the listed blocks only
     if (!o->B_ready || o->nbf_p != nbf_p) {
         const size_t rows = (size_t)naux * nbf_p;
         if ((rc = oz_alloc((void**)&o->rowmax, rows * 8, err)) || (rc = oz_alloc((void**)&o->sA, rows * 4, err)) ||
-            (rc = oz_alloc((void**)&o->Bd, rows * nbf_p * NSL, err)))
+            (rc = oz_alloc((void**)&o->Bd, (size_t)naux * o->nnz * I8_BLOCK, err)))
             return rc;
         cudaMemsetAsync(o->rowmax, 0, rows * 8, s);
         if (L.ntiles > 0)
             oz_rowmax_kernel<<<(unsigned)((size_t)naux * L.ntiles), 256, 0, s>>>(B, L.ntiles, L.tI, L.tJ, nbf_p, o->rowmax);
-        oz_split_B_kernel<<<(unsigned)((size_t)naux * nmb * nkb), 256, 0, s>>>(B, nbf, L.nT, L.ntiles, L.map, nbf_p,
-                                                                               o->rowmax, o->sA, o->Bd);
+        oz_split_B_kernel<<<(unsigned)((size_t)naux * o->nnz), 256, 0, s>>>(
+            B, nbf, L.nT, L.ntiles, L.map, nbf_p, o->nnz, o->d_blk_mb, o->d_mb_kb, o->d_mb_ptr, o->rowmax, o->sA, o->Bd);
         o->nbf_p = nbf_p;
         o->B_ready = true;
     }
@@ -1314,9 +1368,11 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, int nbf, int na
         ta.ngroups = ngroups;
         ta.kdim_b = kdim_b;
         ta.stages = tr_stages;
-        ta.nrun = (nkb * MK + TR_RUN_K - 1) / TR_RUN_K;
+        ta.mb_ptr = o->d_mb_ptr;
+        ta.mb_kb = o->d_mb_kb;
+        ta.nnz = o->nnz;
         ta.ncols = ncols;
-        ta.run_kb = (nkb + ta.nrun - 1) / ta.nrun;
+        ta.run_kb = TR_RUN_K / MK;
         ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;
         ta.n_items = nq * nmb * nchunk;
         ta.err = o->err;

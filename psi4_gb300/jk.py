@@ -79,6 +79,10 @@ class DFJKEngine:
         rows = np.ascontiguousarray(rows, dtype=np.float64)
         self._check(self.L.gdfjk_upload_B_block(self.h, _p(rows), int(q0), int(rows.shape[0])))
 
+    def trim(self):
+        """Release the tensor-core forms' derived copies of B (rebuilt on next use)."""
+        self._check(self.L.gdfjk_trim(self.h))
+
     def upload_device_block(self, ptr: int, q0: int, nq: int):
         """Rows q0 .. q0+nq-1 of the packed triangle already in device memory."""
         self._check(self.L.gdfjk_upload_B_device_block(self.h, ctypes.c_void_p(ptr), int(q0), int(nq)))

@@ -140,3 +140,32 @@ def test_emulated_anchor_in_precision_schedule(ints_built, jk_built):
     r = rhf(jk, *args, e_conv=1e-10, d_conv=1e-8, schedule=PrecisionSchedule(fp64_precision="fp64-emulated"))
     print(f"schedule with emulated FP64 builds: {r.energy:.12f} vs FP64 {e64:.12f}")
     assert abs(r.energy - e64) < 1e-9
+
+
+def test_emulated_block_sparse(jk_built):
+    """A banded pair mask (nbf 640: 10 x 10 tiles, about a third stored): the int8 digits of B
+    are kept only for the 128 x 32 blocks that touch a stored tile, and the half-transform
+    walks only those.  Compared with the native FP64 K of the same engine; `trim` releases the
+    digit copy, which is rebuilt identically."""
+    torch = pytest.importorskip("torch")
+    nbf, naux, nocc = 640, 96, 40
+    idx = np.arange(nbf)
+    mask = (np.abs(idx[:, None] - idx[None, :]) < 90).astype(np.uint8)
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    r, c = np.tril_indices(nbf)
+    tri = torch.from_numpy(mask[r, c].astype(np.float64)).to(dev)
+    Bt = torch.randn((naux, tri.numel()), dtype=torch.float64, device=dev, generator=g) * 0.05 * tri
+    eng = DFJKEngine(nbf, naux, mask)
+    eng.upload_device_block(Bt.data_ptr(), 0, naux // 2)
+    eng.upload_device_block(Bt[naux // 2:].data_ptr(), naux // 2, naux - naux // 2)
+    C = np.random.default_rng(4).standard_normal((nbf, nocc)) * 0.2
+    _, K64, _ = eng.compute(C, mode=abi.DO_K)
+    _, Ke, _ = eng.compute(C, mode=abi.DO_K | abi.EMULATED)
+    err = np.abs(Ke - K64).max()
+    print(f"block-sparse emulated K: max|K| {np.abs(K64).max():.3e} max|dK| {err:.2e}")
+    assert err < TOL + 1e-11 * np.abs(K64).max()
+    eng.trim()
+    _, Ke2, _ = eng.compute(C, mode=abi.DO_K | abi.EMULATED)
+    assert np.array_equal(Ke, Ke2)
