@@ -218,3 +218,80 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
 
 def core_hamiltonian(ints):
     return ints.kinetic() + ints.potential()
+
+
+@dataclass
+class UHFResult:
+    energy: float
+    energies: list
+    iterations: int
+    converged: bool
+    Ca: np.ndarray
+    Cb: np.ndarray
+    Da: np.ndarray
+    Db: np.ndarray
+    nalpha: int
+    nbeta: int
+    timings: dict = field(default_factory=dict)
+    log: list = field(default_factory=list)
+
+
+def uhf(jk, H, S, nalpha, nbeta, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, diis_start=1, fail_on_maxiter=True,
+        verbose=False) -> UHFResult:
+    """Unrestricted HF through the same JK object: psi4's ``UHF::form_G`` pushes the alpha and
+    beta occupied orbitals as two lr-symmetric densities and reads J[0] + J[1], K[0], K[1]
+    (psi4/src/psi4/libscf_solver/uhf.cc:184-230); ``compute_E`` (uhf.cc:361-410):
+
+        E = E_nuc + sum_s tr(D_s H) + 1/2 sum_s tr(D_s J) - 1/2 sum_s tr(D_s K_s),  F_s = H + J - K_s
+
+    Core guess, DIIS on the stacked alpha/beta orbital gradients, convergence as ``rhf``."""
+    X = orthogonalizer(S)
+    t0 = time.perf_counter()
+    eps, Cp = np.linalg.eigh(X.T @ H @ X)
+    Ca = Cb = X @ Cp
+    diis = DIIS()
+    E_old = 0.0
+    energies, log = [], []
+    t_jk = 0.0
+    converged = False
+    it = 0
+    Da = Db = None
+    for it in range(1, maxiter + 1):
+        Ca_occ = np.ascontiguousarray(Ca[:, :nalpha])
+        Cb_occ = np.ascontiguousarray(Cb[:, :nbeta])
+        Da, Db = Ca_occ @ Ca_occ.T, Cb_occ @ Cb_occ.T
+        jk.C_clear()
+        jk.C_left_add(Ca_occ)
+        jk.C_left_add(Cb_occ)
+        tj = time.perf_counter()
+        jk.compute()
+        t_jk += time.perf_counter() - tj
+        Js, Ks = jk.J(), jk.K()
+        J = np.asarray(Js[0]) + np.asarray(Js[1])
+        Ka, Kb = np.asarray(Ks[0]), np.asarray(Ks[1])
+        Fa, Fb = H + J - Ka, H + J - Kb
+        E = (e_nuc + np.vdot(Da + Db, H) + 0.5 * np.vdot(Da + Db, J) - 0.5 * np.vdot(Da, Ka)
+             - 0.5 * np.vdot(Db, Kb))
+        energies.append(float(E))
+        ga = X.T @ (Fa @ Da @ S - S @ Da @ Fa) @ X
+        gb = X.T @ (Fb @ Db @ S - S @ Db @ Fb) @ X
+        dnorm = float(np.sqrt(0.5 * (np.mean(ga * ga) + np.mean(gb * gb))))
+        dE = E - E_old
+        log.append({"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm})
+        if verbose:
+            print(f"  @UHF iter {it:3d}: {E:20.14f} {dE: .3e} {dnorm: .3e}")
+        if abs(dE) < e_conv and dnorm < d_conv:
+            converged = True
+            break
+        E_old = E
+        F2 = np.stack((Fa, Fb))
+        if it >= diis_start:
+            diis.add(F2, np.stack((ga, gb)))
+            F2 = diis.extrapolate() if len(diis.F) >= 2 else F2
+        Ca = X @ np.linalg.eigh(X.T @ F2[0] @ X)[1]
+        Cb = X @ np.linalg.eigh(X.T @ F2[1] @ X)[1]
+    res = UHFResult(energies[-1], energies, it, converged, Ca, Cb, Da, Db, nalpha, nbeta,
+                    {"total_s": time.perf_counter() - t0, "jk_s": t_jk}, log)
+    if not converged and fail_on_maxiter:
+        raise SCFConvergenceError(f"Could not converge UHF iterations in {maxiter} iterations.", res)
+    return res

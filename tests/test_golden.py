@@ -29,3 +29,16 @@ def test_scf5_df_rhf_singlet_o2(ints_built):
     assert abs(r.energy - ref["energy"]) < ref["tolerance"], (r.energy, ref["energy"])
     # tighter than the reference test's own 1e-6: the restatement reproduces it to ~1e-9
     assert abs(r.energy - ref["energy"]) < 5e-9
+
+
+def test_scf5_df_uhf_triplet_o2(ints_built):
+    """Triplet O2 UHF with the MemDF JK restatement (UHF::form_G pushes alpha and beta
+    orbitals through the same JK object) against the reference's stored DF energy."""
+    from psi4_gb300.scf import uhf
+
+    ref = reference_values()["scf5_triplet_uhf_df"]
+    mol, pb, ab, ints, df = system("o2", "cc-pvtz")
+    jk = OracleJK(df.to_pQq(), df.sparsity, df.nbf, df.naux)
+    r = uhf(jk, core_hamiltonian(ints), ints.overlap(), ref["nalpha"], ref["nbeta"], mol.nuclear_repulsion_energy())
+    assert abs(r.energy - ref["energy"]) < ref["tolerance"]
+    assert abs(r.energy - ref["energy"]) < 5e-9  # reproduced to ~1e-9
