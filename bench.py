@@ -369,11 +369,12 @@ def run_gpu(args):
         except Exception as ex:  # reported, not hidden
             out["mixed"] = {"unavailable": str(ex)[:300]}
 
+    # the headline engine's device memory goes back before other configurations are built
+    eng.close()
+    del C, J, K
+    torch.cuda.empty_cache()
     if args.extra and rank == 0:
         # other configurations (synthetic B of their shapes): FP64 build and the precision form
-        eng.close()
-        del C, J, K
-        torch.cuda.empty_cache()
         out["extra_configs"] = {}
         for cfg in [c for c in args.extra.split(",") if c]:
             try:
@@ -389,7 +390,8 @@ def run_gpu(args):
         out["cpu_baseline"] = cpu_baseline(nbf, naux, nocc, budget_s=args.cpu_budget)
     if rank == 0 and args.scf:
         try:
-            out["scf"] = measure_scf(args.scf_config)
+            out["scf"] = (measure_scf_device_B(args.scf_config, dev) if args.scf_config in ("c2", "c3")
+                          else measure_scf(args.scf_config))
         except Exception as ex:
             out["scf"] = {"unavailable": str(ex)[:300]}
     if rank == 0:
@@ -600,6 +602,78 @@ def measure_screened(cfg, dev, args, peaks):
     return out
 
 
+def measure_scf_device_B(cfg, dev):
+    """SCF time-to-converge on real integrals of a large configuration: (P|mn) from the host
+    integrals in blocks of aux rows, B = J^-1/2 (P|mn) accumulated on the device (a plain FP64
+    library GEMM, initialisation only), uploaded into the engine's tiles; then the SCF in native
+    FP64, the emulated FP64 form and the precision form."""
+    import torch
+
+    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.dfhelper import DEFAULT_CONDITION, prepare_sparsity, metric_power
+    from psi4_gb300.ints import Integrals
+    from psi4_gb300.jk import DFJKEngine, GpuDFJK
+    from psi4_gb300.molecule import water_cluster
+    from psi4_gb300.scf import PrecisionSchedule, core_hamiltonian, rhf
+
+    gen, basis, desc = CONFIGS[cfg]
+    mol = water_cluster(*gen["lattice"], seed=0)
+    pb = BasisSet.build(mol, basis)
+    ab = BasisSet.fitting_for(mol, pb)
+    nbf, naux = pb.nbf, ab.nbf
+    t0 = time.perf_counter()
+    ints = Integrals(mol, pb, ab)
+    fun_max, shell_max = ints.schwarz()
+    sp = prepare_sparsity(fun_max, shell_max, 1e-12, naux)
+    Jm = torch.from_numpy(metric_power(ints.metric(), -0.5, DEFAULT_CONDITION)).to(dev)
+    r, c = np.tril_indices(nbf)
+    keep = torch.from_numpy(sp.pair_mask[r, c].astype(np.float64)).to(dev)
+    npair = keep.numel()
+    Bdev = torch.zeros((naux, npair), dtype=torch.float64, device=dev)
+    t_ints = t_gemm = 0.0
+    blk = 128
+    for p0 in range(0, naux, blk):
+        p1 = min(naux, p0 + blk)
+        ta = time.perf_counter()
+        A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
+        t_ints += time.perf_counter() - ta
+        tg = time.perf_counter()
+        Ad = torch.from_numpy(A).to(dev) * keep
+        Bdev.addmm_(Jm[:, p0:p1].contiguous(), Ad)
+        torch.cuda.synchronize()
+        t_gemm += time.perf_counter() - tg
+    eng = DFJKEngine(nbf, naux, sp.pair_mask, device=dev.index or 0)
+    eng.upload_device(Bdev.data_ptr())
+    del Bdev, Jm, keep
+    torch.cuda.empty_cache()
+    H, S = core_hamiltonian(ints), ints.overlap()
+    t_init = time.perf_counter() - t0
+    nocc = mol.nelectron // 2
+    e_nuc = mol.nuclear_repulsion_energy()
+    jk = GpuDFJK.from_engine(eng)
+    out = {"workload": desc + " (real integrals, e_conv 1e-10, d_conv 1e-8, core guess)", "nbf": nbf, "naux": naux,
+           "nocc": nocc, "init_s": t_init, "init_three_index_host_s": t_ints, "init_metric_gemm_device_s": t_gemm}
+    for name, prec, sched in (("fp64_emulated", "fp64-emulated", None),
+                              ("precision_form", None, PrecisionSchedule(fp64_precision="fp64-emulated")),
+                              ("fp64", "fp64", None)):
+        jk.reset_incremental()
+        if prec:
+            jk.set_precision(prec)
+        jk.set_incremental(False)
+        ts = time.perf_counter()
+        rr = rhf(jk, H, S, nocc, e_nuc, schedule=sched)
+        out[name] = {"energy": rr.energy, "iterations": rr.iterations, "seconds": time.perf_counter() - ts,
+                     "jk_seconds": rr.timings["jk_s"]}
+        if sched is not None:
+            out[name].update({"mixed_builds": sched.n_mixed, "fp64_builds": sched.n_fp64})
+    out["abs_energy_difference_emulated_vs_fp64"] = abs(out["fp64_emulated"]["energy"] - out["fp64"]["energy"])
+    out["abs_energy_difference_precision_vs_fp64"] = abs(out["precision_form"]["energy"] - out["fp64"]["energy"])
+    out["time_to_converge_speedup_emulated"] = out["fp64"]["seconds"] / out["fp64_emulated"]["seconds"]
+    out["time_to_converge_speedup_precision_form"] = out["fp64"]["seconds"] / out["precision_form"]["seconds"]
+    eng.close()
+    return out
+
+
 def measure_scf(cfg):
     """SCF time-to-converge on real integrals: FP64-GPU form vs the precision form."""
     from psi4_gb300.basis import BasisSet
@@ -692,7 +766,8 @@ def main():
     ap.add_argument("--fp64-form", default="emulated", choices=["emulated", "native"],
                     help="the headline FP64-accurate build: emulated on BF16 tensor cores or native FP64")
     ap.add_argument("--scf", type=int, default=1)
-    ap.add_argument("--scf-config", default="c4", choices=["c1", "c4"])
+    ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
+                    help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
     ap.add_argument("--extra", default="c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
     args = ap.parse_args()
     if args.warmup < 3:

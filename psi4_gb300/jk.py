@@ -42,6 +42,7 @@ class DFJKEngine:
     def __init__(self, nbf: int, naux: int, pair_mask: np.ndarray | None = None, device: int = 0, flags: int = 0):
         self.L = _native.jk_lib()
         self.nbf, self.naux = int(nbf), int(naux)
+        self.device = int(device)
         h = ctypes.c_void_p()
         self._mask = None
         if pair_mask is not None:
@@ -221,6 +222,14 @@ class GpuDFJK:
     def from_tensor(df: DFTensor, device: int = 0) -> "GpuDFJK":
         return GpuDFJK(df_tensor=df, device=device)
 
+    @staticmethod
+    def from_engine(engine: "DFJKEngine") -> "GpuDFJK":
+        """A JK object over an engine whose B is already uploaded (e.g. B built on the device
+        in blocks); initialize() is then a no-op."""
+        jk = GpuDFJK(device=engine.device)
+        jk.engine = engine
+        return jk
+
     def name(self):
         return "GpuDFJK"
 
@@ -266,6 +275,8 @@ class GpuDFJK:
 
     def initialize(self):
         """preiterations(): build B on the host, upload it to HBM once."""
+        if self.engine is not None and self.df is None:
+            return
         if self.df is None:
             self.df = build_df_tensor(self.molecule, self.primary, self.aux, self.cutoff, self.condition)
         df = self.df
