@@ -42,3 +42,35 @@ def test_scf5_df_uhf_triplet_o2(ints_built):
     r = uhf(jk, core_hamiltonian(ints), ints.overlap(), ref["nalpha"], ref["nbeta"], mol.nuclear_repulsion_energy())
     assert abs(r.energy - ref["energy"]) < ref["tolerance"]
     assert abs(r.energy - ref["energy"]) < 5e-9  # reproduced to ~1e-9
+
+
+def _rhf_energy_zm(zm, basis, jk_factory=None):
+    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.dfhelper import build_df_tensor
+    from psi4_gb300.ints import Integrals
+    from psi4_gb300.molecule import zmatrix
+
+    mol = zmatrix(zm)
+    pb = BasisSet.build(mol, basis)
+    ab = BasisSet.fitting_for(mol, pb)
+    ints = Integrals(mol, pb, ab)
+    df = build_df_tensor(mol, pb, ab, ints=ints)
+    jk = jk_factory(df) if jk_factory else OracleJK(df.to_pQq(), df.sparsity, df.nbf, df.naux)
+    return rhf(jk, core_hamiltonian(ints), ints.overlap(), mol.nelectron // 2, mol.nuclear_repulsion_energy(),
+               e_conv=1e-12, d_conv=1e-10), mol
+
+
+@pytest.mark.parametrize("basis", ["cc-pvdz", "cc-pvtz"])
+def test_dfmp2_2_h2_df_scf(ints_built, basis):
+    """H2 DF-SCF energies stored (and compared to 10 decimals) in the reference's dfmp2-2."""
+    ref = reference_values()["dfmp2_2_h2"]
+    r, mol = _rhf_energy_zm(ref["zmatrix"], basis)
+    assert abs(mol.nuclear_repulsion_energy() - ref["nuclear_repulsion"]) < 1e-12
+    assert abs(r.energy - ref["energy"][basis]) < ref["tolerance"]
+
+
+def test_dfomp2_1_water_df_scf(ints_built):
+    ref = reference_values()["dfomp2_1_water"]
+    r, _ = _rhf_energy_zm(ref["zmatrix"], ref["basis"])
+    assert abs(r.energy - ref["energy"]) < ref["tolerance"]
+    assert abs(r.energy - ref["energy"]) < 1e-9  # reproduced to ~2e-10
