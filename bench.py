@@ -768,7 +768,7 @@ def main():
     ap.add_argument("--scf", type=int, default=1)
     ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
                     help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
-    ap.add_argument("--extra", default="c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
+    ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
