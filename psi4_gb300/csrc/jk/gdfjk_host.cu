@@ -185,12 +185,12 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
             CK(cudaEventRecord(h->ev[3], s));
         } else if (mode & GDFJK_MIXED) {
             if (nonsym) return set_err(h, GDFJK_ERR_ARG, "mixed-precision K needs an lr-symmetric density");
-            rc = mixed_build_K(h->mixed, h->B, L, h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
+            rc = mixed_build_K(h->mixed, h->B, L, h->map.data(), h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
                                h->ev[3], s, h->err);
             if (rc == GDFJK_ERR_OOM) {  // give the emulated form's caches back and retry once
                 CK(cudaStreamSynchronize(s));
                 oz_release(h->oz);
-                rc = mixed_build_K(h->mixed, h->B, L, h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
+                rc = mixed_build_K(h->mixed, h->B, L, h->map.data(), h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
                                    h->ev[3], s, h->err);
             }
             if (rc) return rc;
@@ -632,7 +632,7 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
         CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
     } else if (mode & GDFJK_DO_K) {
         CK(cudaEventRecord(h->ev[2], s));
-        rc = mixed_k_factor(h->mixed, h->B, layout_of(h), h->nbf, h->naux, h->dCrin, std::max(ldu, 1), npos, nu - npos,
+        rc = mixed_k_factor(h->mixed, h->B, layout_of(h), h->map.data(), h->nbf, h->naux, h->dCrin, std::max(ldu, 1), npos, nu - npos,
                             (mode & GDFJK_RESET) ? 0 : 1, h->dK, h->ev[3], s, h->err);
         if (rc) return rc;
         CK(cudaEventRecord(h->ev[4], s));

@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "block_lists.h"
 #include "gdfjk.h"
 #include "mixed.cuh"
 #include "tc_common.cuh"
@@ -68,6 +69,11 @@ struct TcArgs {
     int n_items;  // work items of this launch
     int nbuf;     // TMEM accumulators (2 overlaps the epilogue with the next item)
     int* err;
+    // transform: the listed k blocks of each 128-row block (blocks of B that touch a stored
+    // tile), mb_kb[mb_ptr[mb] .. mb_ptr[mb+1]); the split copy of B holds only those
+    const int* mb_ptr;
+    const int* mb_kb;
+    int nnz, nmb;
 };
 
 __device__ __forceinline__ uint32_t pack_bf162(float a, float b) {
@@ -88,8 +94,9 @@ __device__ __forceinline__ void work_item(const TcArgs& a, int item, int& a_row,
     if (MODE == MODE_TRANSFORM) {
         a_row = item * MM;
         b_row = a.n_off;
-        kb0 = 0;
-        nkb = a.nbf_p / MK;
+        const int mb = item % a.nmb;
+        kb0 = a.mb_ptr[mb];                  // first list entry of this row block
+        nkb = a.mb_ptr[mb + 1] - kb0;        // listed k blocks
         tile = item;
         split = 0;
     } else {
@@ -150,11 +157,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
             const __nv_bfloat16 *pah, *pal, *pbh, *pbl, *pch = nullptr, *pcl = nullptr;
             size_t stepb;
             if (MODE == MODE_TRANSFORM) {
-                const size_t nkbB = a.nbf_p / MK;
-                pah = a.Bsh + ((size_t)(a_row / MM) * nkbB + kb0) * blkA;
-                pal = a.Bsl + ((size_t)(a_row / MM) * nkbB + kb0) * blkA;
-                pbh = a.Uth + (size_t)kb0 * a.nu_pad * MK + (size_t)b_row * MK;
-                pbl = a.Utl + (size_t)kb0 * a.nu_pad * MK + (size_t)b_row * MK;
+                const size_t Q = (size_t)item / a.nmb;
+                pah = a.Bsh + (Q * a.nnz + kb0) * blkA;  // the listed blocks of this row block, in order
+                pal = a.Bsl + (Q * a.nnz + kb0) * blkA;
+                pbh = a.Uth + (size_t)b_row * MK;        // + kb * nu_pad * MK per listed k block
+                pbl = a.Utl + (size_t)b_row * MK;
                 stepb = (size_t)a.nu_pad * MK;
             } else {
                 const size_t nkbt = a.kdim / MK;
@@ -179,10 +186,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
                 pah += blkA;
                 pal += blkA;
                 if (MODE == MODE_TRANSFORM) {
-                    tc::bulk_load(st + a_bytes, pbh, (uint32_t)b_bytes, &full[s]);
-                    tc::bulk_load(st + a_bytes + b_bytes, pbl, (uint32_t)b_bytes, &full[s]);
-                    pbh += stepb;
-                    pbl += stepb;
+                    const size_t kof = (size_t)a.mb_kb[kb0 + kb] * stepb;
+                    tc::bulk_load(st + a_bytes, pbh + kof, (uint32_t)b_bytes, &full[s]);
+                    tc::bulk_load(st + a_bytes + b_bytes, pbl + kof, (uint32_t)b_bytes, &full[s]);
                 } else {
                     tc::bulk_load(st + a_bytes, pbh, A_TILE_BYTES, &full[s]);
                     tc::bulk_load(st + a_bytes + A_TILE_BYTES, pch, A_TILE_BYTES, &full[s]);
@@ -330,13 +336,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
 }
 
 // ---------------------------------------------------------------- helper kernels
-// Dense BF16 hi/lo slices of B (both triangles) from the FP64 tiles: rows (Q, m), columns n.
+// BF16 hi/lo slices of B (both triangles) from the FP64 tiles, rows (Q, m), for the listed
+// 128 x 32 blocks only (those that touch a stored tile): block (Q, entry) at
+// (Q * nnz + entry) * 4096 elements, pre-swizzled.  One CUDA block per row (Q, m).
 __global__ void split_B_kernel(const double* __restrict__ B, int naux, int nbf, int nT, int ntiles,
-                               const int* __restrict__ map, int nbf_p, __nv_bfloat16* __restrict__ Bh,
+                               const int* __restrict__ map, int nbf_p, const int* __restrict__ mb_ptr,
+                               const int* __restrict__ mb_kb, int nnz, __nv_bfloat16* __restrict__ Bh,
                                __nv_bfloat16* __restrict__ Bl) {
     size_t row = blockIdx.x;  // Q * nbf_p + m
     int Q = (int)(row / nbf_p), m = (int)(row % nbf_p);
-    for (int n = threadIdx.x; n < nbf_p; n += blockDim.x) {
+    const int mb = m / MM, p0 = mb_ptr[mb], cnt = mb_ptr[mb + 1] - p0;
+    for (int e = threadIdx.x; e < cnt * MK; e += blockDim.x) {
+        const int p = e / MK, c = e % MK;
+        const int n = mb_kb[p0 + p] * MK + c;
         double v = 0.0;
         if (m < nbf && n < nbf) {
             int I = m / TILE, J = n / TILE;
@@ -349,8 +361,8 @@ __global__ void split_B_kernel(const double* __restrict__ B, int naux, int nbf, 
         }
         __nv_bfloat16 h = __double2bfloat16(v);
         // pre-swizzled 8 KB blocks (128 rows x 32 k): the shared-memory image of an operand tile
-        size_t blk = ((row / MM) * (size_t)(nbf_p / MK) + (size_t)(n / MK)) * (MM * MK);
-        size_t off = blk + tc::swz_offset((uint32_t)(row % MM), (uint32_t)((n % MK) / 8)) / 2 + (n % 8);
+        size_t blk = ((size_t)Q * nnz + p0 + p) * (MM * MK);
+        size_t off = blk + tc::swz_offset((uint32_t)(m % MM), (uint32_t)(c / 8)) / 2 + (c % 8);
         Bh[off] = h;
         Bl[off] = __double2bfloat16(v - (double)__bfloat162float(h));
     }
@@ -437,13 +449,16 @@ struct MixedState {
     int* d_tile_of_block = nullptr;
     int tiles_nbf_p = 0, ntiles_c = 0, ncb = 0;
     __nv_bfloat16* zero_blk = nullptr;
+    int* d_mb_ptr = nullptr;  // listed blocks of B (block_lists.h)
+    int* d_mb_kb = nullptr;
+    int nnz = 0, lists_nbf_p = 0;
 };
 
 MixedState* mixed_create() { return new MixedState(); }
 
 static void free_all(MixedState* m) {
     void* ps[] = {m->Bh, m->Bl, m->Uh, m->Ul, m->Xh, m->Xl, m->part, m->Kacc, m->err, m->d_tiles, m->d_tile_of_block,
-                  m->zero_blk};
+                  m->zero_blk, m->d_mb_ptr, m->d_mb_kb};
     for (void* p : ps)
         if (p) cudaFree(p);
     m->Bh = m->Bl = m->Uh = m->Ul = m->Xh = m->Xl = nullptr;
@@ -453,6 +468,8 @@ static void free_all(MixedState* m) {
     m->d_tiles = nullptr;
     m->d_tile_of_block = nullptr;
     m->zero_blk = nullptr;
+    m->d_mb_ptr = m->d_mb_kb = nullptr;
+    m->lists_nbf_p = 0;
     m->tiles_nbf_p = 0;
     m->U_cap = m->X_cap = m->part_cap = m->Kacc_cap = 0;
     m->B_ready = false;
@@ -499,9 +516,9 @@ static int dalloc_bytes(void** p, size_t bytes, std::string& err) {
 
 // K_inc (written into K, nbf x nbf) = sum_Q B_Q (U+ U+^T - U- U-^T) B_Q; if `accumulate`,
 // the running K is added and updated.
-int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf, int naux, const double* U, int ldu,
-                   int npos, int nneg, int accumulate, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
-                   std::string& err) {
+int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux,
+                   const double* U, int ldu, int npos, int nneg, int accumulate, double* K, cudaEvent_t ev_transform_done,
+                   cudaStream_t s, std::string& err) {
     int rc;
     const int nbf_p = round_up(nbf, MM);
     if (!m->err) {
@@ -512,11 +529,26 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         if ((rc = dalloc_bytes((void**)&m->zero_blk, A_TILE_BYTES, err))) return rc;
         cudaMemsetAsync(m->zero_blk, 0, A_TILE_BYTES, s);
     }
+    if (m->lists_nbf_p != nbf_p) {
+        const BlockLists bl = build_block_lists(map_host, L.nT, nbf_p, MM, MK, TILE);
+        if (bl.kb.empty()) {
+            err = "mixed: B has no stored tiles";
+            return GDFJK_ERR_ARG;
+        }
+        if ((rc = dalloc_bytes((void**)&m->d_mb_ptr, bl.ptr.size() * sizeof(int), err)) ||
+            (rc = dalloc_bytes((void**)&m->d_mb_kb, bl.kb.size() * sizeof(int), err)))
+            return rc;
+        cudaMemcpy(m->d_mb_ptr, bl.ptr.data(), bl.ptr.size() * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(m->d_mb_kb, bl.kb.data(), bl.kb.size() * sizeof(int), cudaMemcpyHostToDevice);
+        m->nnz = (int)bl.kb.size();
+        m->lists_nbf_p = nbf_p;
+        m->B_ready = false;
+    }
     if (!m->B_ready || m->nbf_p != nbf_p) {
-        size_t bytes = (size_t)naux * nbf_p * nbf_p * 2;
+        size_t bytes = (size_t)naux * m->nnz * (MM * MK) * 2;
         if ((rc = dalloc_bytes((void**)&m->Bh, bytes, err)) || (rc = dalloc_bytes((void**)&m->Bl, bytes, err))) return rc;
-        split_B_kernel<<<(unsigned)((size_t)naux * nbf_p), 256, 0, s>>>(B, naux, nbf, L.nT, L.ntiles, L.map, nbf_p, m->Bh,
-                                                                       m->Bl);
+        split_B_kernel<<<(unsigned)((size_t)naux * nbf_p), 256, 0, s>>>(B, naux, nbf, L.nT, L.ntiles, L.map, nbf_p,
+                                                                       m->d_mb_ptr, m->d_mb_kb, m->nnz, m->Bh, m->Bl);
         m->nbf_p = nbf_p;
         m->B_ready = true;
     }
@@ -572,6 +604,10 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
         ta.Bsl = m->Bl;
         ta.Uth = m->Uh;
         ta.Utl = m->Ul;
+        ta.mb_ptr = m->d_mb_ptr;
+        ta.mb_kb = m->d_mb_kb;
+        ta.nnz = m->nnz;
+        ta.nmb = nbf_p / MM;
         // one 128-row tile per item; two TMEM accumulators when they fit, so the epilogue of one
         // item overlaps the MMAs of the next
         ta.n_mtiles = (int)((size_t)naux * nbf_p / MM);
@@ -663,13 +699,13 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, int nbf,
     return GDFJK_OK;
 }
 
-int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, int nbf, int nbf_pad, int naux,
-                  const double* Cpad, int nocc, int nocc_pad, int mode, double* K, cudaEvent_t ev_transform_done,
+int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, const int* map_host, int nbf, int nbf_pad,
+                  int naux, const double* Cpad, int nocc, int nocc_pad, int mode, double* K, cudaEvent_t ev_transform_done,
                   cudaStream_t stream, std::string& err) {
     (void)nbf_pad;
     (void)mode;
     // a full build: U = C_occ, all columns positive
-    return mixed_k_factor(m, B, L, nbf, naux, Cpad, nocc_pad, nocc, 0, 0, K, ev_transform_done, stream, err);
+    return mixed_k_factor(m, B, L, map_host, nbf, naux, Cpad, nocc_pad, nocc, 0, 0, K, ev_transform_done, stream, err);
 }
 
 int mixed_set_base(MixedState* m, const double* K, int nbf, cudaStream_t s, std::string& err) {

@@ -45,6 +45,7 @@
 #include <string>
 #include <vector>
 
+#include "block_lists.h"
 #include "gdfjk.h"
 #include "oz.cuh"
 #include "tc_common.cuh"
@@ -1221,20 +1222,10 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     }
     // ---- the (row block, k block) pairs of B that touch a stored tile (the tile map is fixed)
     if (o->lists_nbf_p != nbf_p) {
-        std::vector<int> ptr(nmb + 1, 0), kbs, bmb;
-        for (int mb = 0; mb < nmb; ++mb) {
-            for (int kb = 0; kb < nkb; ++kb) {
-                const int J = (kb * MK) / TILE;
-                bool any = false;
-                for (int I = 2 * mb; I <= 2 * mb + 1 && !any; ++I)
-                    if (I < L.nT && J < L.nT) any = map_host[(I >= J ? I : J) * L.nT + (I >= J ? J : I)] >= 0;
-                if (any) {
-                    kbs.push_back(kb);
-                    bmb.push_back(mb);
-                }
-            }
-            ptr[mb + 1] = (int)kbs.size();
-        }
+        const BlockLists bl = build_block_lists(map_host, L.nT, nbf_p, MM, MK, TILE);
+        const std::vector<int>& ptr = bl.ptr;
+        const std::vector<int>& kbs = bl.kb;
+        const std::vector<int>& bmb = bl.mb;
         if (kbs.empty()) {
             err = "emulated FP64: B has no stored tiles";
             return GDFJK_ERR_ARG;
