@@ -188,3 +188,12 @@ def dense_jk(B_dense, D, C_left=None, C_right=None):
         Xr = np.einsum("qmn,ni->qmi", B_dense, C_right)
         K = np.einsum("qmi,qni->mn", Xl, Xr)
     return J, K
+
+
+def memdfjk_memory_estimate(sparsity, nbf, naux, qshell_max, nthreads=1):
+    """MemDFJK::memory_estimate (psi4/src/psi4/libfock/MemDFJK.cc:65-69) -> DFHelper::get_core_size
+    -> AO_core (psi4/src/psi4/lib3index/dfhelper.cc:216-236), in doubles, for the STORE path
+    without wK: the sparse AO tensor (big_skips[nbf] = naux * significant pairs), the metric,
+    one nbf^2 C buffer per thread and three nbf^2 * Qshell_max temporaries (Qshell_max = the
+    most functions in one aux shell, dfhelper.cc:92)."""
+    return int(sparsity.big_skips[nbf]) + naux * naux + nthreads * nbf * nbf + 3 * nbf * nbf * qshell_max

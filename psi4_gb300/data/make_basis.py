@@ -3,7 +3,7 @@
 The basis-set data are the published correlation-consistent sets (Dunning 1989 for
 cc-pVXZ on H/C/O; Weigend 2002 for the cc-pVXZ-JKFIT fitting sets) as distributed
 with psi4 in ``psi4/share/psi4/basis/*.gbs`` (Gaussian94 format).  Only the elements
-the seeded workloads need (H, C, O) are kept.  The files are data, not code; each
+the seeded workloads and the reference's stored test values need (H, C, O, Ar) are kept.  The files are data, not code; each
 JSON records the source file and the element list.
 
 Usage (in a checkout with the psi4 sources available)::
@@ -20,7 +20,7 @@ import sys
 
 AM = {"S": 0, "P": 1, "D": 2, "F": 3, "G": 4, "H": 5, "I": 6}
 BASES = ["cc-pvdz", "cc-pvdz-jkfit", "cc-pvtz", "cc-pvtz-jkfit"]
-ELEMENTS = ["H", "C", "O"]
+ELEMENTS = ["H", "C", "O", "Ar"]
 
 
 def _num(tok):

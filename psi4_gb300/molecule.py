@@ -22,7 +22,8 @@ import numpy as np
 BOHR2ANGSTROM = 0.52917721067
 ANGSTROM2BOHR = 1.0 / BOHR2ANGSTROM
 
-Z_OF = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10}
+Z_OF = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10, "Na": 11, "Mg": 12,
+        "Al": 13, "Si": 14, "P": 15, "S": 16, "Cl": 17, "Ar": 18}
 
 
 @dataclass

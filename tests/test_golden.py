@@ -74,3 +74,26 @@ def test_dfomp2_1_water_df_scf(ints_built):
     r, _ = _rhf_energy_zm(ref["zmatrix"], ref["basis"])
     assert abs(r.energy - ref["energy"]) < ref["tolerance"]
     assert abs(r.energy - ref["energy"]) < 1e-9  # reproduced to ~2e-10
+
+
+def test_jkmemory_memdf_ccpvdz(ints_built):
+    """MemDFJK's memory estimate for Ar5 / cc-pVDZ (tests/pytests/test_jkmemory.py, -n1): an
+    exact integer that pins the Schwarz sparsity (significant function pairs) and the
+    size formula."""
+    import numpy as np
+
+    from oracle.dfjk_ref import memdfjk_memory_estimate
+    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.dfhelper import prepare_sparsity
+    from psi4_gb300.ints import Integrals
+    from psi4_gb300.molecule import ANGSTROM2BOHR, Molecule
+
+    ref = reference_values()["jkmemory"]
+    xyz = np.array(ref["geometry_angstrom"], dtype=float) * ANGSTROM2BOHR
+    mol = Molecule(ref["symbols"], xyz)
+    pb = BasisSet.build(mol, "cc-pvdz")
+    ab = BasisSet.fitting_for(mol, pb)
+    fun_max, shell_max = Integrals(mol, pb, ab).schwarz()
+    sp = prepare_sparsity(fun_max, shell_max, 1e-12, ab.nbf)
+    qmax = int(ab.nfunc_per_shell.max())
+    assert memdfjk_memory_estimate(sp, pb.nbf, ab.nbf, qmax, nthreads=1) == ref["mem_df_ccpvdz_doubles"]
