@@ -19,7 +19,7 @@ import os
 import sys
 
 AM = {"S": 0, "P": 1, "D": 2, "F": 3, "G": 4, "H": 5, "I": 6}
-BASES = ["cc-pvdz", "cc-pvdz-jkfit", "cc-pvtz", "cc-pvtz-jkfit"]
+BASES = ["cc-pvdz", "cc-pvdz-jkfit", "cc-pvtz", "cc-pvtz-jkfit", "cc-pv5z", "cc-pv5z-jkfit"]
 ELEMENTS = ["H", "C", "O", "Ar"]
 
 

@@ -76,14 +76,16 @@ def test_dfomp2_1_water_df_scf(ints_built):
     assert abs(r.energy - ref["energy"]) < 1e-9  # reproduced to ~2e-10
 
 
-def test_jkmemory_memdf_ccpvdz(ints_built):
-    """MemDFJK's memory estimate for Ar5 / cc-pVDZ (tests/pytests/test_jkmemory.py, -n1): an
-    exact integer that pins the Schwarz sparsity (significant function pairs) and the
-    size formula."""
+@pytest.mark.parametrize("basis,key", [("cc-pvdz", "mem_df_ccpvdz_doubles"), ("cc-pv5z", "mem_df_ccpv5z_doubles")])
+def test_jkmemory_memdf(ints_built, basis, key):
+    """MemDFJK's memory estimate for Ar5 (tests/pytests/test_jkmemory.py, -n1): an exact integer
+    that pins the Schwarz sparsity (significant function pairs of the primary basis) and the
+    size formula.  The fitting set enters only through its function count and largest shell,
+    read from the basis data (cc-pV5Z-JKFIT has i functions, beyond this integral code)."""
     import numpy as np
 
     from oracle.dfjk_ref import memdfjk_memory_estimate
-    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.basis import BasisSet, _load
     from psi4_gb300.dfhelper import prepare_sparsity
     from psi4_gb300.ints import Integrals
     from psi4_gb300.molecule import ANGSTROM2BOHR, Molecule
@@ -91,9 +93,10 @@ def test_jkmemory_memdf_ccpvdz(ints_built):
     ref = reference_values()["jkmemory"]
     xyz = np.array(ref["geometry_angstrom"], dtype=float) * ANGSTROM2BOHR
     mol = Molecule(ref["symbols"], xyz)
-    pb = BasisSet.build(mol, "cc-pvdz")
-    ab = BasisSet.fitting_for(mol, pb)
-    fun_max, shell_max = Integrals(mol, pb, ab).schwarz()
-    sp = prepare_sparsity(fun_max, shell_max, 1e-12, ab.nbf)
-    qmax = int(ab.nfunc_per_shell.max())
-    assert memdfjk_memory_estimate(sp, pb.nbf, ab.nbf, qmax, nthreads=1) == ref["mem_df_ccpvdz_doubles"]
+    pb = BasisSet.build(mol, basis)
+    aux_shells = _load(basis + "-jkfit")["elements"]["Ar"]
+    naux = len(ref["symbols"]) * sum(2 * sh["l"] + 1 for sh in aux_shells)
+    qmax = max(2 * sh["l"] + 1 for sh in aux_shells)
+    fun_max, shell_max = Integrals(mol, pb, pb).schwarz()
+    sp = prepare_sparsity(fun_max, shell_max, 1e-12, naux)
+    assert memdfjk_memory_estimate(sp, pb.nbf, naux, qmax, nthreads=1) == ref[key]
