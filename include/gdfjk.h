@@ -53,7 +53,8 @@ enum {
     GDFJK_RESET = 16,      /* forget the incremental history (next build is a full build)      */
     GDFJK_EMULATED = 32    /* K to FP64 accuracy from BF16 tensor-core products of 7-bit digit
                               slices (Ozaki splitting, exact FP32 level sums, double-float
-                              epilogue); lr-symmetric densities; ignored with GDFJK_MIXED      */
+                              epilogue); lr-symmetric densities, nocc <= 1024; ignored with
+                              GDFJK_MIXED                                                      */
 };
 
 /* Create an engine on CUDA device `device` for nbf basis functions and naux fitting

@@ -1255,6 +1255,11 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         o->nbf_p = nbf_p;
         o->B_ready = true;
     }
+    if (nocc_pad > RUN_K) {
+        // one aux function's columns must fit one exact contraction run (levels 0-3 provably exact)
+        err = "emulated FP64: nocc above " + std::to_string(RUN_K) + " is not supported (use the native FP64 K)";
+        return GDFJK_ERR_ARG;
+    }
     // ---- digits of C^T, in column chunks of <= 80 (six accumulators in the 512 TMEM columns,
     // three pipeline stages in shared memory)
     const int nocc_p = nocc_pad;

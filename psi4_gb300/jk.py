@@ -319,7 +319,10 @@ class GpuDFJK:
             mode |= abi.MIXED
             if self.incremental:
                 mode |= abi.INCREMENTAL
-        emu = abi.EMULATED if (self.precision == "fp64-emulated" and lr_symmetric) else 0
+        # the emulated form serves lr-symmetric densities with up to 1024 occupied columns; others
+        # take the native FP64 K
+        emu = abi.EMULATED if (self.precision == "fp64-emulated" and lr_symmetric and
+                               all(C.shape[1] <= 1024 for C in self._Cl)) else 0
         mode |= emu
         self._J, self._K, self._D = [], [], []
         if self.precision in ("fp64", "fp64-emulated") and self.incremental and lr_symmetric and self.do_K and \

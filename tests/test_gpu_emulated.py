@@ -12,7 +12,7 @@ import pytest
 
 from oracle import dfjk_ref
 from psi4_gb300 import _jkabi as abi
-from psi4_gb300.jk import DFJKEngine, GpuDFJK
+from psi4_gb300.jk import DFJKEngine, GdfjkError, GpuDFJK
 from tests.helpers import random_orbitals, reference_values, system
 
 pytestmark = pytest.mark.gpu
@@ -85,10 +85,11 @@ def test_emulated_determinism_and_batches(ints_built, jk_built, monkeypatch):
 
 
 def test_emulated_long_k_runs(jk_built):
-    """nbf 1100: the half-transform's k range is cut into two exact accumulation runs.
+    """nbf 2100 (2176 padded, over the 2048 terms of one run): the half-transform's k range is
+    cut into two accumulation runs, the second added to the first in double-float.
     Synthetic B on the device; reference: plain torch FP64."""
     torch = pytest.importorskip("torch")
-    nbf, naux, nocc = 1100, 48, 96
+    nbf, naux, nocc = 2100, 16, 96
     dev = torch.device("cuda:0")
     g = torch.Generator(device=dev)
     g.manual_seed(7)
@@ -169,3 +170,18 @@ def test_emulated_block_sparse(jk_built):
     eng.trim()
     _, Ke2, _ = eng.compute(C, mode=abi.DO_K | abi.EMULATED)
     assert np.array_equal(Ke, Ke2)
+
+
+def test_emulated_rejects_wide_occupation(jk_built):
+    """More than 1024 occupied columns would overrun one exact contraction run: refused with a
+    clear error (GpuDFJK routes such densities to the native FP64 K)."""
+    nbf, naux = 128, 8
+    eng = DFJKEngine(nbf, naux, None)
+    rng = np.random.default_rng(1)
+    r, c = np.tril_indices(nbf)
+    eng.upload_qtri(rng.standard_normal((naux, r.size)) * 0.01)
+    C = rng.standard_normal((nbf, 1040)) * 0.01
+    with pytest.raises(GdfjkError, match="nocc above 1024"):
+        eng.compute(C, mode=abi.DO_K | abi.EMULATED)
+    _, K, _ = eng.compute(C, mode=abi.DO_K)  # the engine stays usable
+    assert np.isfinite(K).all()
