@@ -612,9 +612,10 @@ def measure_screened(cfg, dev, args, peaks):
 
 def measure_scf_device_B(cfg, dev):
     """SCF time-to-converge on real integrals of a large configuration: (P|mn) from the host
-    integrals in blocks of aux rows, B = J^-1/2 (P|mn) accumulated on the device (a plain FP64
-    library GEMM, initialisation only), uploaded into the engine's tiles; then the SCF in native
-    FP64, the emulated FP64 form and the precision form."""
+    integrals in blocks of aux rows, copied into one device array; B = J^-1/2 (P|mn) by the
+    engine's tensor-core metric contraction (checked against the FP64 library GEMM on a slice
+    of columns), uploaded into the engine's tiles; then the SCF in native FP64, the emulated
+    FP64 form and the precision form."""
     import torch
 
     from psi4_gb300.basis import BasisSet
@@ -633,12 +634,12 @@ def measure_scf_device_B(cfg, dev):
     ints = Integrals(mol, pb, ab)
     fun_max, shell_max = ints.schwarz()
     sp = prepare_sparsity(fun_max, shell_max, 1e-12, naux)
-    Jm = torch.from_numpy(metric_power(ints.metric(), -0.5, DEFAULT_CONDITION)).to(dev)
+    Jm = torch.from_numpy(metric_power(ints.metric(), -0.5, DEFAULT_CONDITION)).to(dev).contiguous()
     r, c = np.tril_indices(nbf)
     keep = torch.from_numpy(sp.pair_mask[r, c].astype(np.float64)).to(dev)
     npair = keep.numel()
-    Bdev = torch.zeros((naux, npair), dtype=torch.float64, device=dev)
-    t_ints = t_gemm = 0.0
+    Pdev = torch.empty((naux, npair), dtype=torch.float64, device=dev)
+    t_ints = t_copy = 0.0
     blk = 128
     for p0 in range(0, naux, blk):
         p1 = min(naux, p0 + blk)
@@ -646,21 +647,41 @@ def measure_scf_device_B(cfg, dev):
         A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
         t_ints += time.perf_counter() - ta
         tg = time.perf_counter()
-        Ad = torch.from_numpy(A).to(dev) * keep
-        Bdev.addmm_(Jm[:, p0:p1].contiguous(), Ad)
+        Pdev[p0:p1] = torch.from_numpy(A).to(dev) * keep
         torch.cuda.synchronize()
-        t_gemm += time.perf_counter() - tg
+        t_copy += time.perf_counter() - tg
+    del keep
     eng = DFJKEngine(nbf, naux, sp.pair_mask, device=dev.index or 0)
+    Bdev = torch.empty((naux, npair), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    tg = time.perf_counter()
+    eng.metric_contract(Jm.data_ptr(), Pdev.data_ptr(), npair, Bdev.data_ptr())
+    t_gemm = time.perf_counter() - tg
+    # the FP64 library GEMM on a slice of columns, for accuracy and its own rate
+    ncheck = min(npair, 65536)
+    torch.cuda.synchronize()
+    tf = time.perf_counter()
+    Bref = Jm @ Pdev[:, :ncheck]
+    torch.cuda.synchronize()
+    t_fp64_slice = time.perf_counter() - tf
+    metric_check = {"columns": ncheck, "max_abs_dB": (Bdev[:, :ncheck] - Bref).abs().max().item(),
+                    "max_abs_B": Bref.abs().max().item(), "fp64_library_gemm_s": t_fp64_slice,
+                    "fp64_library_gemm_s_scaled_to_all_columns": t_fp64_slice * npair / ncheck}
+    del Bref, Pdev
+    torch.cuda.empty_cache()
     eng.upload_device(Bdev.data_ptr())
-    del Bdev, Jm, keep
+    del Bdev, Jm
     torch.cuda.empty_cache()
     H, S = core_hamiltonian(ints), ints.overlap()
-    t_init = time.perf_counter() - t0
+    t_init = time.perf_counter() - t0 - t_fp64_slice  # without the accuracy check
     nocc = mol.nelectron // 2
     e_nuc = mol.nuclear_repulsion_energy()
     jk = GpuDFJK.from_engine(eng)
     out = {"workload": desc + " (real integrals, e_conv 1e-10, d_conv 1e-8, core guess)", "nbf": nbf, "naux": naux,
-           "nocc": nocc, "init_s": t_init, "init_three_index_host_s": t_ints, "init_metric_gemm_device_s": t_gemm}
+           "nocc": nocc, "init_s": t_init, "init_three_index_host_s": t_ints, "init_three_index_copy_s": t_copy,
+           "init_metric_contraction_device_s": t_gemm,
+           "metric_contraction_fp64_tflops": 2.0 * naux * naux * npair / t_gemm / 1e12,
+           "metric_contraction_check": metric_check}
     for name, prec, sched in (("fp64_emulated", "fp64-emulated", None),
                               ("precision_form", None, PrecisionSchedule(fp64_precision="fp64-emulated")),
                               ("fp64", "fp64", None)):

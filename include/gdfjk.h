@@ -82,6 +82,22 @@ int gdfjk_upload_B_device(gdfjk_t h, const double* B_qtri_device);
 int gdfjk_upload_B_block(gdfjk_t h, const double* B_qtri_rows, int q0, int nq);
 int gdfjk_upload_B_device_block(gdfjk_t h, const double* B_qtri_rows_device, int q0, int nq);
 
+/* The metric contraction B = J^-1/2 (P|mn) on the tensor cores, to FP64 accuracy (the
+ * emulated-FP64 digit products of GDFJK_EMULATED): replaces the naux x naux DGEMM of
+ * DFHelper::contract_metric_AO_core_symm (dfhelper.cc:1653-1678) called from
+ * DFHelper::prepare_AO_core (dfhelper.cc:514-588).  All device buffers, row-major:
+ *   metric  naux x naux (e.g. J^-1/2 from Matrix::power(-0.5, condition), matrix.cc:2370-2415)
+ *   Pmn     naux x ncols, leading dimension ldp >= ncols (the raw 3-index integrals; with
+ *           ncols = nbf(nbf+1)/2 in GDFJK_LAYOUT_QTRI order, B comes out ready for
+ *           gdfjk_upload_B_device)
+ *   B       naux x ncols, leading dimension ldb >= ncols: B = metric Pmn, or B += metric Pmn
+ *           with accumulate != 0 (B must not overlap Pmn)
+ * Runs on the handle's stream with temporary device buffers (the digits of the metric and of
+ * one column chunk of Pmn, GDFJK_OZ_GEMM_CHUNK_GB, default 8 GB) and returns when B is
+ * complete.  The handle's B is not touched. */
+int gdfjk_metric_contract_device(gdfjk_t h, const double* metric, const double* Pmn, int ncols, int64_t ldp, double* B,
+                                 int64_t ldb, int accumulate);
+
 /* One Fock build, host buffers (JK::compute, jk.cc:595-681, for one density):
  *   C_left  nbf x nocc (row-major, leading dimension ldc >= nocc)
  *   C_right nbf x nocc or NULL (NULL = lr-symmetric: D = C_left C_left^T, jk.cc:597-599)

@@ -14,6 +14,7 @@ SIGNATURES = {
     "gdfjk_upload_B_block": (I, [P, P, I, I]),
     "gdfjk_upload_B_device_block": (I, [P, P, I, I]),
     "gdfjk_trim": (I, [P]),
+    "gdfjk_metric_contract_device": (I, [P, P, P, I, ctypes.c_int64, P, ctypes.c_int64, I]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_incremental": (I, [P, P, I, I, P, I, I, I, I, P, P]),

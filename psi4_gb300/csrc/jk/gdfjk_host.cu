@@ -460,6 +460,19 @@ int gdfjk_upload_B_device(gdfjk_t h, const double* Bq) {
     return GDFJK_OK;
 }
 
+int gdfjk_metric_contract_device(gdfjk_t h, const double* metric, const double* Pmn, int ncols, int64_t ldp, double* B,
+                                 int64_t ldb, int accumulate) {
+    if (!h || !metric || !Pmn || !B) return set_err(h, GDFJK_ERR_ARG, "metric_contract_device: null argument");
+    if (ncols < 0 || ldp < ncols || ldb < ncols)
+        return set_err(h, GDFJK_ERR_ARG, "metric_contract_device: invalid column count or leading dimension");
+    CK(cudaSetDevice(h->device));
+    if (!h->oz) h->oz = oz_create();
+    int rc = oz_gemm(h->oz, metric, (size_t)h->naux, Pmn, (size_t)ldp, B, (size_t)ldb, h->naux, ncols, h->naux,
+                     accumulate, h->stream, h->err);
+    if (rc) return set_err(h, rc, "metric_contract_device: " + h->err);
+    return check_device_flag(h);
+}
+
 int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_skips, const int64_t* small_skips,
                    const int64_t* fun_index) {
     if (!h || !B) return set_err(h, GDFJK_ERR_ARG, "upload_B: null argument");

@@ -133,6 +133,38 @@ __device__ __forceinline__ long long fix_f(float x, int E) {
 __device__ __forceinline__ uint32_t digit_field(unsigned long long u, int s) {
     return (uint32_t)(u >> (7 * (NSL - 1 - s))) & 127u;
 }
+
+// The same with NS digits (the general product uses eight): v = round(x 2^(7 NS - 2 - E)),
+// |v| <= 2^(7 NS - 2), so that x = 2^(E-5) sum_s d_s 2^(-7s) whatever NS is.
+template <int NS>
+__device__ __forceinline__ long long fix_dn(double x, int E) {
+    if (E == E_EMPTY) return 0;
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    int ex = (int)((b >> 52) & 0x7FF);
+    unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    if (ex)
+        mant |= 1ull << 52;
+    else
+        ex = 1;
+    const int r = 1075 - (7 * NS - 2) + E - ex;  // >= 6 - 7 (NS - 7) because |x| < 2^E
+    unsigned long long v;
+    if (r <= 0)
+        v = mant << (-r);
+    else
+        v = r >= 64 ? 0ull : ((mant + (1ull << (r - 1))) >> r);
+    return (b >> 63) ? -(long long)v : (long long)v;
+}
+template <int NS>
+__device__ __forceinline__ unsigned long long digit_off() {
+    unsigned long long o = 0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) o = (o << 7) | 64ull;
+    return o;
+}
+template <int NS>
+__device__ __forceinline__ uint32_t digit_field_n(unsigned long long u, int s) {
+    return (uint32_t)(u >> (7 * (NS - 1 - s))) & 127u;
+}
 // BF16 bits of the slice value (f - 64) * 2^(-7s), exact; w = 2^(-7s)
 __device__ __forceinline__ uint32_t field_bf16(uint32_t f, float w) {
     float g = fmaf(__uint_as_float(0x4B000000u | f), w, -8388672.0f * w);
@@ -434,6 +466,53 @@ __device__ __forceinline__ void issue_slice_j(int j, const uint32_t* d, uint32_t
         case 5: issue_slice<NA, 5>(d, a_col, dB, b_step, id, first); break;
         default: issue_slice<NA, 6>(d, a_col, dB, b_step, id, first); break;
     }
+}
+
+// The contraction's form with NS digits and levels up to MAXL: slice J against B slices
+// t <= min(NS - 1, MAXL - J), accumulator min(J + t, NA - 1).
+template <int NS, int NA, int MAXL, int J>
+__device__ __forceinline__ void issue_slice_g(const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step, uint32_t id,
+                                              bool first) {
+    constexpr int TMAX = (NS - 1) < (MAXL - J) ? (NS - 1) : (MAXL - J);
+#pragma unroll
+    for (int ks = 0; ks < MK / 16; ++ks) {
+#pragma unroll
+        for (int t = 0; t <= TMAX; ++t) {
+            const int L = J + t < NA - 1 ? J + t : NA - 1;
+            const uint32_t f = (first && ks == 0 && J == 0 && t <= NA - 1) ? 0u : 1u;
+            mma_bf16_ta(d[L], a_col + (uint32_t)(8 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
+        }
+    }
+}
+template <int NS, int NA, int MAXL>
+__device__ __forceinline__ void issue_slice_gj(int j, const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step,
+                                               uint32_t id, bool first) {
+    static_assert(NS <= 8 && MAXL >= NS - 1, "up to eight digits, every slice used");
+    switch (j) {
+        case 0: issue_slice_g<NS, NA, MAXL, 0>(d, a_col, dB, b_step, id, first); break;
+        case 1: issue_slice_g<NS, NA, MAXL, 1>(d, a_col, dB, b_step, id, first); break;
+        case 2: issue_slice_g<NS, NA, MAXL, 2>(d, a_col, dB, b_step, id, first); break;
+        case 3: issue_slice_g<NS, NA, MAXL, 3>(d, a_col, dB, b_step, id, first); break;
+        case 4: issue_slice_g<NS, NA, MAXL, 4>(d, a_col, dB, b_step, id, first); break;
+        case 5: issue_slice_g<NS, NA, MAXL, 5>(d, a_col, dB, b_step, id, first); break;
+        case 6: issue_slice_g<NS, NA, MAXL, 6>(d, a_col, dB, b_step, id, first); break;
+        default: issue_slice_g<NS, NA, MAXL, (NS > 7 ? 7 : 6)>(d, a_col, dB, b_step, id, first); break;
+    }
+}
+
+// a[0] + ... + a[NA-1]: NA - 1 exact level sums and the tail, as an FP32 pair
+template <int NA>
+__device__ __forceinline__ void combine_n(const float* a, float& hi, float& lo) {
+    float s = a[0], l = 0.f;
+#pragma unroll
+    for (int i = 1; i < NA - 1; ++i) {
+        float e;
+        two_sum(s, a[i], s, e);
+        l = __fadd_rn(l, e);
+    }
+    l = __fadd_rn(l, a[NA - 1]);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 
 // Persistent, warp-specialised: warp 0 lane 0 bulk-copies one k block (int8 A + BF16 C^T) per
@@ -772,25 +851,35 @@ __global__ void __launch_bounds__(256) oz_split_X_kernel(const float2* __restric
 
 // ---------------------------------------------------------------- contraction
 struct CtArgs {
-    const __nv_bfloat16* Xd;  // [mb][kbt][7][128][32]
-    const float* Sx;          // [group][nbf_p]
-    const int2* tiles;        // (128-row block, 64-row block) of the lower triangle
-    int ntiles, nsplit, gps, ngroups, G, nocc_p, nq, nbf_p;
-    size_t nkbt;
-    double* part;  // [nsplit][ntiles][128][64]
+    const __nv_bfloat16* Xd;  // row operand digits [mb][kbt][7][128][32]
+    const __nv_bfloat16* Yd;  // column operand digits, same layout (= Xd for K = X X^T)
+    const float* Sx;          // row weights [group][lds_x]
+    const float* Sy;          // column weights [group][lds_y]
+    const int2* tiles;        // (128-row block, 64-column block): the lower triangle for K
+    int ntiles, nsplit, gps, ngroups;
+    int kpg, nkb;             // k blocks per group (one accumulation run), k blocks in all
+    int lds_x, lds_y;
+    size_t nkbt;              // k-block stride of the digit arrays
+    double* part;             // [nsplit][ntiles][128][64] (out == nullptr)
+    double* out;              // general product: out[m][n] (+)= result for m < M, n < N
+    size_t ldo;
+    int M, N, accumulate;
     int stages, n_items;
     int* err;
 };
 
-// Stage per k block: [7 A slices, 128 rows | 7 B slices, 64 rows].  The copier warps move each
-// A slice into a TMEM slot (the MMAs take A from tensor memory and only B from shared memory);
-// six accumulators (levels 0-4 exact, tail 5-6) at TMEM columns 0..383, A slots at 400..511.
+// Stage per k block: [NS A slices, 128 rows | NS B slices, 64 rows].  The copier warps move
+// each A slice into a TMEM slot (the MMAs take A from tensor memory and only B from shared
+// memory).  K = X X^T: 7 digits, six accumulators (levels 0-4 exact, tail 5-6) at TMEM columns
+// 0..383, seven A slots at 400..511.  The general product (metric contraction): 8 digits,
+// levels <= 8, seven accumulators (levels 0-5 exact, tail 6-8) at 0..447, four A slots.
 constexpr int CT_NACC = NACC;
-constexpr int CT_OFF_B = NSL * BF_SLICE;                  // 56 KB
-constexpr int CT_STAGE = CT_OFF_B + NSL * CT_N * MK * 2;  // + 28 KB
 constexpr int CT_ASLOTS = 7;
-constexpr int CT_ACOL0 = 512 - CT_ASLOTS * 16;
 constexpr int CT_THREADS = 448;  // producer, MMA, 8 epilogue warps, 4 copier warps
+__host__ __device__ constexpr int ct_stage_bytes(int ns) { return ns * BF_SLICE + ns * CT_N * MK * 2; }
+constexpr int CT_STAGE = ct_stage_bytes(NSL);  // 84 KB
+constexpr int GM_NS = 8, GM_NACC = 7, GM_MAXL = 8, GM_ASLOTS = 4;
+static_assert(GM_NACC * CT_N + GM_ASLOTS * 16 <= 512 && CT_NACC * CT_N + CT_ASLOTS * 16 <= 512, "TMEM columns");
 
 __device__ __forceinline__ void ct_item(const CtArgs& a, int item, int& tile, int& g0, int& g1) {
     const int split = item / a.ntiles;  // split-major: concurrent CTAs share one k window in L2
@@ -798,17 +887,21 @@ __device__ __forceinline__ void ct_item(const CtArgs& a, int item, int& tile, in
     g0 = split * a.gps;
     g1 = min(a.ngroups, g0 + a.gps);
 }
-__device__ __forceinline__ int ct_kb0(const CtArgs& a, int g) { return g * a.G * a.nocc_p / MK; }
-__device__ __forceinline__ int ct_kb1(const CtArgs& a, int g) { return min(a.nq, (g + 1) * a.G) * a.nocc_p / MK; }
+__device__ __forceinline__ int ct_kb0(const CtArgs& a, int g) { return g * a.kpg; }
+__device__ __forceinline__ int ct_kb1(const CtArgs& a, int g) { return min(a.nkb, (g + 1) * a.kpg); }
 
+template <int NS, int NA, int MAXL, int ASLOTS, bool DIRECT>
 __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs a) {
+    constexpr int OFF_B = NS * BF_SLICE;
+    constexpr int STAGE = ct_stage_bytes(NS);
+    constexpr int ACOL0 = 512 - ASLOTS * 16;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * CT_STAGE);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * STAGE);
     uint64_t* empty = full + a.stages;
-    uint64_t* afull = empty + a.stages;    // [CT_ASLOTS]
-    uint64_t* aempty = afull + CT_ASLOTS;  // [CT_ASLOTS]
-    uint64_t* tfull = aempty + CT_ASLOTS;  // [2]
+    uint64_t* afull = empty + a.stages;    // [ASLOTS]
+    uint64_t* aempty = afull + ASLOTS;  // [ASLOTS]
+    uint64_t* tfull = aempty + ASLOTS;  // [2]
     uint64_t* tempty = tfull + 2;          // [2]
     uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
@@ -818,7 +911,7 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        for (int r = 0; r < CT_ASLOTS; ++r) {
+        for (int r = 0; r < ASLOTS; ++r) {
             tc::mbar_init(&afull[r], 128);
             tc::mbar_init(&aempty[r], 1);
         }
@@ -846,8 +939,8 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             int tile, g0, g1;
             ct_item(a, item, tile, g0, g1);
             const int2 tb = a.tiles[tile];
-            const __nv_bfloat16* pa = a.Xd + (size_t)tb.x * a.nkbt * NSL * blk;
-            const __nv_bfloat16* pb = a.Xd + (size_t)(tb.y / 2) * a.nkbt * NSL * blk + (size_t)(tb.y % 2) * (CT_N * MK);
+            const __nv_bfloat16* pa = a.Xd + (size_t)tb.x * a.nkbt * NS * blk;
+            const __nv_bfloat16* pb = a.Yd + (size_t)(tb.y / 2) * a.nkbt * NS * blk + (size_t)(tb.y % 2) * (CT_N * MK);
             for (int g = g0; ok && g < g1; ++g) {
                 const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
                 for (int kb = kb0; kb < kb1; ++kb, ++kg) {
@@ -855,11 +948,11 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                         ok = false;
                         break;
                     }
-                    uint8_t* st = smem + (size_t)s * CT_STAGE;
-                    tc::mbar_arrive_expect_tx(&full[s], (uint32_t)CT_STAGE);
-                    tc::bulk_load(st, pa + (size_t)kb * NSL * blk, (uint32_t)(NSL * BF_SLICE), &full[s]);
-                    for (int t = 0; t < NSL; ++t)
-                        tc::bulk_load(st + CT_OFF_B + t * (CT_N * MK * 2), pb + ((size_t)kb * NSL + t) * blk, CT_N * MK * 2,
+                    uint8_t* st = smem + (size_t)s * STAGE;
+                    tc::mbar_arrive_expect_tx(&full[s], (uint32_t)STAGE);
+                    tc::bulk_load(st, pa + (size_t)kb * NS * blk, (uint32_t)(NS * BF_SLICE), &full[s]);
+                    for (int t = 0; t < NS; ++t)
+                        tc::bulk_load(st + OFF_B + t * (CT_N * MK * 2), pb + ((size_t)kb * NS + t) * blk, CT_N * MK * 2,
                                       &full[s]);
                     if (++s == a.stages) {
                         s = 0;
@@ -888,18 +981,18 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                         ok = false;
                         break;
                     }
-                    const uint8_t* st = smem + (size_t)s * CT_STAGE;
+                    const uint8_t* st = smem + (size_t)s * STAGE;
 #pragma unroll 1
-                    for (int j0 = 0; ok && j0 < NSL; j0 += 2) {
-                        const int nj = NSL - j0 < 2 ? NSL - j0 : 2;
+                    for (int j0 = 0; ok && j0 < NS; j0 += 2) {
+                        const int nj = NS - j0 < 2 ? NS - j0 : 2;
                         int slot[2] = {0, 0};
                         for (int jj = 0; jj < nj; ++jj, ++used) {
-                            if (used >= CT_ASLOTS && !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
+                            if (used >= ASLOTS && !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
                                 ok = false;
                                 break;
                             }
                             slot[jj] = r;
-                            if (++r == CT_ASLOTS) {
+                            if (++r == ASLOTS) {
                                 r = 0;
                                 pr ^= 1u;
                             }
@@ -917,7 +1010,7 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                                 o[4 * c + 2] = v.z;
                                 o[4 * c + 3] = v.w;
                             }
-                            tmem_st16(lane_base + (uint32_t)(CT_ACOL0 + 16 * slot[jj]), o);
+                            tmem_st16(lane_base + (uint32_t)(ACOL0 + 16 * slot[jj]), o);
                         }
                         tmem_wait_st();
                         tc::tc_fence_before();
@@ -948,27 +1041,27 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                     break;
                 }
                 tc::tc_fence_after();
-                uint32_t d[CT_NACC];
+                uint32_t d[NA];
 #pragma unroll
-                for (int L = 0; L < CT_NACC; ++L) d[L] = tmem + (uint32_t)(L * CT_N);
+                for (int L = 0; L < NA; ++L) d[L] = tmem + (uint32_t)(L * CT_N);
                 const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
                 for (int kb = kb0; ok && kb < kb1; ++kb) {
                     if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
                         ok = false;
                         break;
                     }
-                    const uint64_t dB = tc::sdesc_kmajor(smem_base + (uint32_t)(s * CT_STAGE + CT_OFF_B));
+                    const uint64_t dB = tc::sdesc_kmajor(smem_base + (uint32_t)(s * STAGE + OFF_B));
                     const bool first = kb == kb0;
 #pragma unroll
-                    for (int j = 0; j < NSL; ++j) {
+                    for (int j = 0; j < NS; ++j) {
                         if (!tc::mbar_wait(&afull[r], pr, abort_flag, a.err)) {
                             ok = false;
                             break;
                         }
                         tc::tc_fence_after();
-                        issue_slice_j<CT_NACC>(j, d, tmem + (uint32_t)(CT_ACOL0 + 16 * r), dB, b_step, id, first);
+                        issue_slice_gj<NS, NA, MAXL>(j, d, tmem + (uint32_t)(ACOL0 + 16 * r), dB, b_step, id, first);
                         tc::mma_commit(&aempty[r]);
-                        if (++r == CT_ASLOTS) {
+                        if (++r == ASLOTS) {
                             r = 0;
                             pr ^= 1u;
                         }
@@ -1010,22 +1103,25 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                     break;
                 }
                 tc::tc_fence_after();
-                const float rs = a.Sx[(size_t)g * a.nbf_p + m];
-                const float* cs = a.Sx + (size_t)g * a.nbf_p + n0;
+                const float rs = a.Sx[(size_t)g * a.lds_x + m];
+                const float* cs = a.Sy + (size_t)g * a.lds_y + n0;
 #pragma unroll
                 for (int c0 = 0; c0 < HC; c0 += 4) {
-                    uint32_t v[CT_NACC][4];
+                    uint32_t v[NA][4];
 #pragma unroll
-                    for (int L = 0; L < CT_NACC; ++L)
+                    for (int L = 0; L < NA; ++L)
                         tc::tmem_ld4_nowait(lane_base + (uint32_t)(L * CT_N + half * HC + c0), v[L]);
                     tc::tmem_wait_ld();
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        float acc[CT_NACC];
+                        float acc[NA];
 #pragma unroll
-                        for (int L = 0; L < CT_NACC; ++L) acc[L] = __uint_as_float(v[L][j]);
+                        for (int L = 0; L < NA; ++L) acc[L] = __uint_as_float(v[L][j]);
                         float hi, lo;
-                        combine6(acc, hi, lo);
+                        if constexpr (NA == 6)
+                            combine6(acc, hi, lo);
+                        else
+                            combine_n<NA>(acc, hi, lo);
                         const float sc = rs * cs[c0 + j];
                         df_add(RH[c0 + j], RL[c0 + j], hi * sc, lo * sc);
                     }
@@ -1035,11 +1131,25 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                 if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[0]);
             }
             if (!ok) break;
-            double* dst = a.part + (((size_t)(item / a.ntiles) * a.ntiles + tile) * MM + r) * CT_N + half * HC;
+            if constexpr (DIRECT) {
+                // general product: the rows and columns that exist, (+)= into out
+                if (m < a.M) {
+                    double* dst = a.out + (size_t)m * a.ldo + n0;
+                    const int nv = min(HC, a.N - n0);
 #pragma unroll
-            for (int c = 0; c < HC; c += 2)
-                *reinterpret_cast<double2*>(dst + c) =
-                    make_double2((double)RH[c] + (double)RL[c], (double)RH[c + 1] + (double)RL[c + 1]);
+                    for (int c = 0; c < HC; ++c)
+                        if (c < nv) {
+                            const double v = (double)RH[c] + (double)RL[c];
+                            dst[c] = a.accumulate ? dst[c] + v : v;
+                        }
+                }
+            } else {
+                double* dst = a.part + (((size_t)(item / a.ntiles) * a.ntiles + tile) * MM + r) * CT_N + half * HC;
+#pragma unroll
+                for (int c = 0; c < HC; c += 2)
+                    *reinterpret_cast<double2*>(dst + c) =
+                        make_double2((double)RH[c] + (double)RL[c], (double)RH[c + 1] + (double)RL[c + 1]);
+            }
         }
     }
     __syncwarp();
@@ -1070,6 +1180,123 @@ __global__ void oz_reduce_kernel(const double* __restrict__ part, int nsplit, in
         if (accumulate) s += K[m * nbf + n];
         K[m * nbf + n] = s;
         K[n * nbf + m] = s;
+    }
+}
+
+// ---------------------------------------------------------------- general product C (+)= A B
+// Digits for the contraction kernel run as a general GEMM (the metric contraction
+// B = J^-1/2 (P|mn)): A (M x K, row-major) gives the row operand with one exponent per
+// (row, group of RUN_K k), B (K x N, row-major) the column operand, transposed, with one
+// exponent per (column, group).  Both land in [block of 128][kbt][8][128][32] pre-swizzled
+// BF16 slices; rows/columns past M/N and k past K are zero digits.  Eight digits (55-bit
+// fixed point) and levels up to 8, with level 5 exact as well: J^-1/2 has entries ~50x the
+// largest element of B that cancel in the product, and the error of the digit form scales
+// with the row and column maxima rather than with each term.
+
+// Exponent and weight of A's row m in group g: one warp per (m, g).
+__global__ void oz_gemm_rowexp_kernel(const double* __restrict__ A, size_t lda, int M, int K, int kw, int ngroups,
+                                      int M_pad, int* __restrict__ Ea, float* __restrict__ Sa) {
+    const int wid = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32), lane = threadIdx.x % 32;
+    if (wid >= M_pad * ngroups) return;
+    const int m = wid % M_pad, g = wid / M_pad;
+    unsigned long long mx = 0;
+    if (m < M) {
+        const int k1 = min(K, (g + 1) * kw);
+        for (int k = g * kw + lane; k < k1; k += 32) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(A[(size_t)m * lda + k]) & 0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) {
+        const int E = exp_of_max_d(mx);
+        Ea[(size_t)g * M_pad + m] = E;
+        Sa[(size_t)g * M_pad + m] = scale_of(E);
+    }
+}
+
+// Exponent and weight of B's column n in group g: one thread per (n, g), coalesced over n.
+__global__ void oz_gemm_colexp_kernel(const double* __restrict__ B, size_t ldb, int N, int K, int kw, int ngroups,
+                                      int N_pad, int* __restrict__ Eb, float* __restrict__ Sb) {
+    const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (id >= (size_t)N_pad * ngroups) return;
+    const int n = (int)(id % N_pad), g = (int)(id / N_pad);
+    unsigned long long mx = 0;
+    if (n < N) {
+        const int k1 = min(K, (g + 1) * kw);
+        for (int k = g * kw; k < k1; ++k) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(B[(size_t)k * ldb + n]) & 0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+    }
+    const int E = exp_of_max_d(mx);
+    Eb[(size_t)g * N_pad + n] = E;
+    Sb[(size_t)g * N_pad + n] = scale_of(E);
+}
+
+// Eight consecutive values -> the GM_NS BF16 slices of their digits, packed in uint4s.
+__device__ __forceinline__ void digits8(const double* x, int E, uint32_t (&w)[GM_NS][4]) {
+    const unsigned long long off = digit_off<GM_NS>();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const unsigned long long uu = (unsigned long long)(fix_dn<GM_NS>(x[j], E) + (long long)off);
+#pragma unroll
+        for (int s = 0; s < GM_NS; ++s) {
+            const uint32_t bits = field_bf16(digit_field_n<GM_NS>(uu, s), slice_weight(s));
+            if (j % 2 == 0)
+                w[s][j / 2] = bits;
+            else
+                w[s][j / 2] |= bits << 16;
+        }
+    }
+}
+__device__ __forceinline__ void store_slices(__nv_bfloat16* base, int r, int c, const uint32_t (&w)[GM_NS][4]) {
+    const uint32_t off = tc::swz_offset((uint32_t)r, (uint32_t)c) / 2;
+#pragma unroll
+    for (int s = 0; s < GM_NS; ++s)
+        *reinterpret_cast<uint4*>(base + (size_t)s * (MM * MK) + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// Row operand: unit = (row, 8 consecutive k); units ordered (block, kb, row, chunk) so that a
+// warp reads 8 rows x 256 contiguous bytes.
+__global__ void __launch_bounds__(256) oz_gemm_split_A_kernel(const double* __restrict__ A, size_t lda, int M, int K,
+                                                              int M_pad, int nkbt, int kpg, const int* __restrict__ Ea,
+                                                              __nv_bfloat16* __restrict__ Xd) {
+    const size_t total = (size_t)M_pad * nkbt * (MK / 8);
+    for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < total; u += (size_t)gridDim.x * blockDim.x) {
+        const int c = (int)(u % (MK / 8));
+        const int r = (int)((u / (MK / 8)) % MM);
+        const size_t bk = u / (MM * (MK / 8));  // mb * nkbt + kb
+        const int kb = (int)(bk % nkbt), mb = (int)(bk / nkbt);
+        const int m = mb * MM + r, k0 = kb * MK + c * 8;
+        const int E = Ea[(size_t)(kb / kpg) * M_pad + m];
+        double x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = (m < M && k0 + j < K) ? A[(size_t)m * lda + k0 + j] : 0.0;
+        uint32_t w[GM_NS][4];
+        digits8(x, E, w);
+        store_slices(Xd + bk * GM_NS * (MM * MK), r, c, w);
+    }
+}
+
+// Column operand (B transposed): unit = (column n, 8 consecutive k); consecutive threads take
+// consecutive columns, so each of the eight row reads is coalesced.
+__global__ void __launch_bounds__(256) oz_gemm_split_Bt_kernel(const double* __restrict__ B, size_t ldb, int N, int K,
+                                                               int N_pad, int nkbt, int kpg, const int* __restrict__ Eb,
+                                                               __nv_bfloat16* __restrict__ Yd) {
+    const size_t total = (size_t)N_pad * nkbt * (MK / 8);
+    for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < total; u += (size_t)gridDim.x * blockDim.x) {
+        const int n = (int)(u % N_pad);
+        const size_t kc = u / N_pad;  // kb * 4 + chunk
+        const int kb = (int)(kc / (MK / 8)), c = (int)(kc % (MK / 8));
+        const int k0 = kb * MK + c * 8;
+        const int E = Eb[(size_t)(kb / kpg) * N_pad + n];
+        double x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = (n < N && k0 + j < K) ? B[(size_t)(k0 + j) * ldb + n] : 0.0;
+        uint32_t w[GM_NS][4];
+        digits8(x, E, w);
+        store_slices(Yd + ((size_t)(n / MM) * nkbt + kb) * GM_NS * (MM * MK), n % MM, c, w);
     }
 }
 
@@ -1199,12 +1426,12 @@ int oz_error_flag(OzState* o, cudaStream_t s) {
     return f;
 }
 
-int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
-               int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err) {
+namespace {
+
+// error word, SM count and kernel attributes, once per state
+int oz_prepare(OzState* o, cudaStream_t s, std::string& err) {
     using namespace oz;
     int rc;
-    const int nbf_p = round_up(nbf, MM);
-    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
     if (!o->err) {
         if ((rc = oz_alloc((void**)&o->err, sizeof(int), err))) return rc;
         cudaMemsetAsync(o->err, 0, sizeof(int), s);
@@ -1217,9 +1444,24 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     }
     if (!o->attrs_set) {
         cudaFuncSetAttribute(oz_transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
-        cudaFuncSetAttribute(oz_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(oz_contract_kernel<GM_NS, GM_NACC, GM_MAXL, GM_ASLOTS, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
         o->attrs_set = true;
     }
+    return GDFJK_OK;
+}
+
+}  // namespace
+
+int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
+               int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err) {
+    using namespace oz;
+    int rc;
+    const int nbf_p = round_up(nbf, MM);
+    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
+    if ((rc = oz_prepare(o, s, err))) return rc;
     // ---- the (row block, k block) pairs of B that touch a stored tile (the tile map is fixed)
     if (o->lists_nbf_p != nbf_p) {
         const BlockLists bl = build_block_lists(map_host, L.nT, nbf_p, MM, MK, TILE);
@@ -1390,22 +1632,24 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         }
         CtArgs ca{};
         ca.Xd = o->Xd;
+        ca.Yd = o->Xd;
         ca.Sx = o->Sx;
+        ca.Sy = o->Sx;
         ca.tiles = o->d_tiles;
         ca.ntiles = o->ntiles;
         ca.nsplit = nsplit;
         ca.gps = gps;
         ca.ngroups = ngroups;
-        ca.G = G;
-        ca.nocc_p = nocc_p;
-        ca.nq = nq;
-        ca.nbf_p = nbf_p;
+        ca.kpg = G * nocc_p / MK;
+        ca.nkb = (int)nkbt;
+        ca.lds_x = ca.lds_y = nbf_p;
         ca.nkbt = nkbt;
         ca.part = o->part;
         ca.stages = ct_stages;
         ca.n_items = o->ntiles * nsplit;
         ca.err = o->err;
-        oz_contract_kernel<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+        oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, false>
+            <<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
         const size_t nl = (size_t)nbf * (nbf + 1) / 2;
         const int blocks = (int)std::min<size_t>((nl + 255) / 256, (size_t)o->num_sms * 16);
         oz_reduce_kernel<<<blocks, 256, 0, s>>>(o->part, nsplit, o->ntiles, nbf, o->d_tob, o->ncb, K, batch > 0 ? 1 : 0);
@@ -1413,6 +1657,139 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         err = std::string("emulated FP64: launch failed: ") + cudaGetErrorString(e);
+        return GDFJK_ERR_CUDA;
+    }
+    return GDFJK_OK;
+}
+
+namespace {
+
+double gemm_chunk_bytes() {
+    const char* s = getenv("GDFJK_OZ_GEMM_CHUNK_GB");
+    double gb = s ? atof(s) : 8.0;
+    if (!(gb > 0.0)) gb = 8.0;
+    return gb * 1e9;
+}
+
+// Work items of one column chunk: every (128-row block, 64-column block) pair, in strips of 16
+// column blocks, row-block-major inside a strip, so that the CTAs working at the same time
+// share a few row blocks of A and 16 column blocks of B in L2.
+std::vector<int2> gemm_tiles(int nmb, int ncb) {
+    constexpr int W = 16;
+    std::vector<int2> tl;
+    tl.reserve((size_t)nmb * ncb);
+    for (int c0 = 0; c0 < ncb; c0 += W)
+        for (int mb = 0; mb < nmb; ++mb)
+            for (int c = c0; c < std::min(ncb, c0 + W); ++c) tl.push_back(make_int2(mb, c));
+    return tl;
+}
+
+// device buffers of one product, released when the call returns
+struct GemmBuffers {
+    void* p[8] = {};
+    ~GemmBuffers() {
+        for (void* q : p)
+            if (q) cudaFree(q);
+    }
+};
+
+}  // namespace
+
+int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb, double* C, size_t ldc, int M, int N,
+            int K, int accumulate, cudaStream_t s, std::string& err) {
+    using namespace oz;
+    int rc;
+    if (M < 0 || N < 0 || K < 1 || !A || !B || !C || lda < (size_t)K || ldb < (size_t)N || ldc < (size_t)N) {
+        err = "emulated FP64 product: invalid sizes or pointers";
+        return GDFJK_ERR_ARG;
+    }
+    if (M == 0 || N == 0) return GDFJK_OK;
+    if ((rc = oz_prepare(o, s, err))) return rc;
+    const int M_pad = round_up(M, MM), K_pad = round_up(K, MK);
+    const int nkbt = K_pad / MK, kpg = RUN_K / MK;
+    const int ngroups = (nkbt + kpg - 1) / kpg;
+    const int nmb = M_pad / MM;
+    // columns per chunk: digits of B (K_pad x 7 BF16 slices) within the chunk budget
+    const double per_col = (double)K_pad * GM_NS * 2.0 + ngroups * 8.0 + (double)nmb * 8.0 / CT_N;
+    long nc = (long)std::floor(gemm_chunk_bytes() / per_col / MM) * MM;
+    nc = std::max<long>(MM, std::min<long>(nc, round_up(N, MM)));
+    GemmBuffers bufs;
+    __nv_bfloat16 *Xd = nullptr, *Yd = nullptr;
+    int *Ea = nullptr, *Eb = nullptr;
+    float *Sa = nullptr, *Sb = nullptr;
+    int2* tiles = nullptr;
+    if ((rc = oz_alloc(&bufs.p[0], (size_t)M_pad * K_pad * GM_NS * 2, err)) ||
+        (rc = oz_alloc(&bufs.p[1], (size_t)ngroups * M_pad * 4, err)) ||
+        (rc = oz_alloc(&bufs.p[2], (size_t)ngroups * M_pad * 4, err)) ||
+        (rc = oz_alloc(&bufs.p[3], (size_t)nc * K_pad * GM_NS * 2, err)) ||
+        (rc = oz_alloc(&bufs.p[4], (size_t)ngroups * nc * 4, err)) ||
+        (rc = oz_alloc(&bufs.p[5], (size_t)ngroups * nc * 4, err)) ||
+        (rc = oz_alloc(&bufs.p[6], (size_t)nmb * (nc / CT_N) * sizeof(int2), err)))
+        return rc;
+    Xd = (__nv_bfloat16*)bufs.p[0];
+    Ea = (int*)bufs.p[1];
+    Sa = (float*)bufs.p[2];
+    Yd = (__nv_bfloat16*)bufs.p[3];
+    Eb = (int*)bufs.p[4];
+    Sb = (float*)bufs.p[5];
+    tiles = (int2*)bufs.p[6];
+    const int ct_stages = std::min(4, (SMEM_BUDGET - SMEM_RESERVE) / ct_stage_bytes(GM_NS));
+    {
+        const size_t warps = (size_t)M_pad * ngroups;
+        oz_gemm_rowexp_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(A, lda, M, K, RUN_K, ngroups, M_pad, Ea,
+                                                                                      Sa);
+        const size_t units = (size_t)M_pad * nkbt * (MK / 8);
+        const int blocks = (int)std::min<size_t>((units + 255) / 256, (size_t)o->num_sms * 16);
+        oz_gemm_split_A_kernel<<<blocks, 256, 0, s>>>(A, lda, M, K, M_pad, nkbt, kpg, Ea, Xd);
+    }
+    int tiles_ncb = -1;
+    for (long c0 = 0; c0 < N; c0 += nc) {
+        const int ncc = (int)std::min<long>(nc, N - c0);
+        const int N_pad = round_up(ncc, MM);
+        const int ncb = N_pad / CT_N;
+        if (ncb != tiles_ncb) {
+            const std::vector<int2> tl = gemm_tiles(nmb, ncb);
+            cudaStreamSynchronize(s);  // the previous chunk's contraction may still read the list
+            cudaMemcpy(tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice);
+            tiles_ncb = ncb;
+        }
+        const size_t cols = (size_t)N_pad * ngroups;
+        oz_gemm_colexp_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, s>>>(B + c0, ldb, ncc, K, RUN_K, ngroups, N_pad, Eb,
+                                                                              Sb);
+        const size_t units = (size_t)N_pad * nkbt * (MK / 8);
+        const int blocks = (int)std::min<size_t>((units + 255) / 256, (size_t)o->num_sms * 16);
+        oz_gemm_split_Bt_kernel<<<blocks, 256, 0, s>>>(B + c0, ldb, ncc, K, N_pad, nkbt, kpg, Eb, Yd);
+        CtArgs ca{};
+        ca.Xd = Xd;
+        ca.Yd = Yd;
+        ca.Sx = Sa;
+        ca.Sy = Sb;
+        ca.tiles = tiles;
+        ca.ntiles = nmb * ncb;
+        ca.nsplit = 1;
+        ca.gps = ngroups;
+        ca.ngroups = ngroups;
+        ca.kpg = kpg;
+        ca.nkb = nkbt;
+        ca.lds_x = M_pad;
+        ca.lds_y = N_pad;
+        ca.nkbt = (size_t)nkbt;
+        ca.part = nullptr;
+        ca.out = C + c0;
+        ca.ldo = ldc;
+        ca.M = M;
+        ca.N = ncc;
+        ca.accumulate = accumulate ? 1 : 0;
+        ca.stages = ct_stages;
+        ca.n_items = ca.ntiles;
+        ca.err = o->err;
+        oz_contract_kernel<GM_NS, GM_NACC, GM_MAXL, GM_ASLOTS, true>
+            <<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the buffers are released on return
+    if (e != cudaSuccess) {
+        err = std::string("emulated FP64 product: ") + cudaGetErrorString(e);
         return GDFJK_ERR_CUDA;
     }
     return GDFJK_OK;

@@ -84,6 +84,18 @@ class DFJKEngine:
         """Release the tensor-core forms' derived copies of B (rebuilt on next use)."""
         self._check(self.L.gdfjk_trim(self.h))
 
+    def metric_contract(self, metric_ptr: int, pmn_ptr: int, ncols: int, out_ptr: int, ldp: int | None = None,
+                        ldb: int | None = None, accumulate: bool = False):
+        """B (+)= metric (P|mn) on the tensor cores to FP64 accuracy, all device pointers:
+        metric naux x naux, (P|mn) naux x ncols (leading dimension ldp), B naux x ncols (ldb);
+        DFHelper::contract_metric_AO_core_symm's product (dfhelper.cc:1653-1678).  With the
+        packed-triangle column order, B is ready for `upload_device`."""
+        ldp = ncols if ldp is None else ldp
+        ldb = ncols if ldb is None else ldb
+        self._check(self.L.gdfjk_metric_contract_device(self.h, ctypes.c_void_p(metric_ptr), ctypes.c_void_p(pmn_ptr),
+                                                        int(ncols), int(ldp), ctypes.c_void_p(out_ptr), int(ldb),
+                                                        1 if accumulate else 0))
+
     def upload_device_block(self, ptr: int, q0: int, nq: int):
         """Rows q0 .. q0+nq-1 of the packed triangle already in device memory."""
         self._check(self.L.gdfjk_upload_B_device_block(self.h, ctypes.c_void_p(ptr), int(q0), int(nq)))
