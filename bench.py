@@ -386,6 +386,14 @@ def run_gpu(args):
                 out["extra_configs"][cfg] = {"unavailable": str(ex)[:300]}
             torch.cuda.empty_cache()
 
+    if rank == 0 and args.host_b:
+        out["host_b"] = {}
+        for cfg in [c for c in args.host_b.split(",") if c]:
+            try:
+                out["host_b"][cfg] = measure_host_b(cfg, dev, args)
+            except Exception as ex:
+                out["host_b"][cfg] = {"unavailable": str(ex)[:300]}
+            torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(nbf, naux, nocc, budget_s=args.cpu_budget)
     if rank == 0 and args.scf:
@@ -520,6 +528,79 @@ def measure_config(cfg, dev, args, peaks):
     free, total = torch.cuda.mem_get_info(dev)
     out["device_memory_in_use_gb"] = (total - free) / 1e9  # all engine buffers of both forms allocated
     eng.close()
+    return out
+
+
+def _host_mem_available():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def measure_host_b(cfg, dev, args):
+    """Builds with B in pinned host (Grace) memory, read by the same kernels over NVLink-C2C,
+    against the same engine with B in HBM: J (two passes over the FP64 tiles of B) and the
+    emulated-FP64 build (its digit copy of B stays in HBM).  Synthetic dense B; skipped when B
+    would take more than a third of the host's available memory."""
+    import torch
+
+    from psi4_gb300 import _jkabi as abi
+    from psi4_gb300.jk import DFJKEngine
+
+    mol, nbf, naux, nocc, desc = workload_sizes(cfg)
+    npair = nbf * (nbf + 1) // 2
+    nT = (nbf + 63) // 64
+    b_bytes = naux * nT * (nT + 1) // 2 * 4096 * 8
+    avail = _host_mem_available()
+    if b_bytes > avail / 3:
+        return {"skipped": f"B {b_bytes / 1e9:.1f} GB is above a third of the available host memory "
+                           f"({avail / 1e9:.1f} GB)"}
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2468)
+    C = torch.randn((nbf, nocc), dtype=torch.float64, device=dev, generator=gen) * 0.1
+    J = torch.empty((nbf, nbf), dtype=torch.float64, device=dev)
+    K = torch.empty_like(J)
+    out = {"workload": desc + " (synthetic B, dense)", "nbf": nbf, "naux": naux, "nocc": nocc,
+           "b_tiles_gb": b_bytes / 1e9, "host_mem_available_gb": avail / 1e9}
+    for tier, flags in (("hbm", 0), ("host", abi.B_HOST)):
+        eng = DFJKEngine(nbf, naux, None, device=dev.index or 0, flags=flags)
+        blk = max(1, min(256, int(4e9 // (npair * 8))))
+        buf = torch.empty((blk, npair), dtype=torch.float64, device=dev)
+        for q0 in range(0, naux, blk):
+            nq = min(blk, naux - q0)
+            buf[:nq].normal_(0.0, 0.02, generator=gen)
+            torch.cuda.synchronize()
+            eng.upload_device_block(buf.data_ptr(), q0, nq)
+        del buf
+        torch.cuda.empty_cache()
+        stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+
+        def run(mode, n):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(n):
+                eng.compute_device(C.data_ptr(), None, nocc, nocc, mode, None, J.data_ptr(), K.data_ptr())
+            e1.record(stream)
+            eng.synchronize()
+            return e0.elapsed_time(e1) / 1e3 / n
+
+        run(abi.DO_J, 2)
+        tj = run(abi.DO_J, max(3, args.steps))
+        em = abi.DO_J | abi.DO_K | abi.EMULATED
+        run(em, 2)
+        te = run(em, max(2, args.steps))
+        out[tier] = {"j_ms": 1e3 * tj, "j_read_gb_per_s": 2 * b_bytes / tj / 1e9,
+                     "emulated_builds_per_s": 1.0 / te, "emulated_ms_per_build": 1e3 * te,
+                     "emulated_phase_ms": eng.timings()}
+        eng.close()
+        torch.cuda.empty_cache()
+    out["emulated_slowdown_host_vs_hbm"] = out["host"]["emulated_ms_per_build"] / out["hbm"]["emulated_ms_per_build"]
     return out
 
 
@@ -798,6 +879,8 @@ def main():
     ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
                     help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
     ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
+    ap.add_argument("--host-b", default="c4",
+                    help="configurations measured with B in pinned host memory (GDFJK_B_HOST), '' for none")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

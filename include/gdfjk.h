@@ -57,9 +57,21 @@ enum {
                               GDFJK_MIXED                                                      */
 };
 
+/* gdfjk_create flags */
+enum {
+    GDFJK_B_HOST = 256  /* keep the FP64 tiles of B in pinned host (Grace) memory mapped into
+                           the GPU's address space; the kernels read them over NVLink-C2C.
+                           For systems whose B does not fit in HBM (psi4's out-of-core
+                           DFHelper, grab_AO, dfhelper.cc:1419-1432); results are identical.
+                           The tensor-core forms' derived copies of B stay in HBM (they are
+                           streamed with bulk copies); where they do not fit, those forms
+                           return GDFJK_ERR_OOM and the native FP64 form still runs       */
+};
+
 /* Create an engine on CUDA device `device` for nbf basis functions and naux fitting
  * functions.  pair_mask (nbf*nbf bytes, symmetric, nullable = every pair significant)
- * is DFHelper's Schwarz function mask (schwarz_fun_index_ != 0, dfhelper.cc:375-386). */
+ * is DFHelper's Schwarz function mask (schwarz_fun_index_ != 0, dfhelper.cc:375-386).
+ * flags: 0 or GDFJK_B_HOST. */
 int gdfjk_create(int device, int nbf, int naux, const unsigned char* pair_mask, int flags, gdfjk_t* out);
 
 /* Upload B from host memory, once (MemDFJK::preiterations -> DFHelper::initialize,
@@ -139,7 +151,8 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
  * device memory back between phases. */
 int gdfjk_trim(gdfjk_t h);
 
-/* Device bytes the engine needs for these sizes (feeds JK::memory_estimate, jk.h:398). */
+/* Device bytes the engine needs for these sizes (feeds JK::memory_estimate, jk.h:398);
+ * flags: mode bits of the forms in use, plus GDFJK_B_HOST (B then not counted). */
 int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes);
 
 /* Timing of the last build in milliseconds (J passes, K half-transform, K contraction). */

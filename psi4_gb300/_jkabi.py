@@ -37,6 +37,8 @@ GDFJK_ERR_TIMEOUT = -5
 GDFJK_ERR_NUMERIC = -6
 GDFJK_ERR_DEVICE = -7
 
+B_HOST = 256  # gdfjk_create flag: B in pinned Grace memory, read over NVLink-C2C
+
 LAYOUT_PQQ = 0
 LAYOUT_QTRI = 1
 

@@ -38,6 +38,14 @@ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 // Record an error message for gdfjk_last_error(NULL) on this thread; returns `code`.
 int report_error(int code, const std::string& msg);
 
+// Memory tiers of the large arrays (B and its derived copies): HBM, or pinned Grace memory
+// mapped into the GPU's address space, which the kernels read coherently over NVLink-C2C
+// (the device pointer is the host pointer).  big_alloc puts `bytes` in host memory when
+// `host`, else in HBM; big_free releases either kind.
+cudaError_t big_alloc(void** p, size_t bytes, bool host);
+void big_free(void* p);
+bool is_host_memory(const void* p);
+
 }  // namespace gdfjk
 
 // kernels (defined in j_kernels.cu / k_fp64.cu); all enqueue on `stream`.

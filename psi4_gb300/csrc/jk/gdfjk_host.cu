@@ -35,6 +35,40 @@ int gdfjk::report_error(int code, const std::string& msg) {
     return code;
 }
 
+cudaError_t gdfjk::big_alloc(void** p, size_t bytes, bool host) {
+    *p = nullptr;
+    if (!host) return cudaMalloc(p, std::max<size_t>(bytes, 16));
+    void* hp = nullptr;
+    cudaError_t e = cudaHostAlloc(&hp, std::max<size_t>(bytes, 16), cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) return e;
+    void* dp = nullptr;
+    e = cudaHostGetDevicePointer(&dp, hp, 0);
+    if (e != cudaSuccess || dp != hp) {  // the kernels take the one pointer (unified addressing)
+        cudaFreeHost(hp);
+        return e != cudaSuccess ? e : cudaErrorInvalidValue;
+    }
+    *p = hp;
+    return cudaSuccess;
+}
+
+bool gdfjk::is_host_memory(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+void gdfjk::big_free(void* p) {
+    if (!p) return;
+    if (is_host_memory(p))
+        cudaFreeHost(p);
+    else
+        cudaFree(p);
+}
+
 struct gdfjk_s {
     int device = 0;
     int nbf = 0, naux = 0, nT = 0, nbf_pad = 0, ntiles = 0;
@@ -105,6 +139,23 @@ int dalloc(gdfjk_t h, T** p, size_t n) {
 }
 
 TileLayout layout_of(gdfjk_t h) { return TileLayout{h->nT, h->ntiles, h->d_tI, h->d_tJ, h->d_map}; }
+
+// the FP64 tiles of B: HBM, or pinned Grace memory with GDFJK_B_HOST
+int alloc_B(gdfjk_t h) {
+    if (h->B) return GDFJK_OK;
+    const size_t bytes = (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS * sizeof(double);
+    const bool host = (h->flags & GDFJK_B_HOST) != 0;
+    cudaError_t e = big_alloc(reinterpret_cast<void**>(&h->B), bytes, host);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        h->B = nullptr;
+        char buf[200];
+        snprintf(buf, sizeof buf, "%s allocation of %.3f GB for B refused (%s)", host ? "pinned host" : "device",
+                 bytes / 1e9, cudaGetErrorString(e));
+        return set_err(h, e == cudaErrorMemoryAllocation ? GDFJK_ERR_OOM : GDFJK_ERR_CUDA, buf);
+    }
+    return GDFJK_OK;
+}
 
 // D/J work buffers and the padded C always; the FP64 X buffers and split-K partials only when
 // `need_x` (the native FP64 K and the backward pass use them; the tensor-core forms do not).
@@ -271,7 +322,7 @@ int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes
     size_t nbf_pad = (size_t)nT * TILE;
     size_t ntiles = (size_t)nT * (nT + 1) / 2;  // upper bound (no screening)
     size_t nocc_pad = (size_t)round_up(max_nocc, 32);
-    size_t b = (size_t)naux * ntiles * TILE_ELEMS * 8;          // B
+    size_t b = (flags & GDFJK_B_HOST) ? 0 : (size_t)naux * ntiles * TILE_ELEMS * 8;  // B (HBM)
     b += nbf_pad * nbf_pad * 8 + 2 * ntiles * TILE_ELEMS * 8;    // D, Dw, Jt
     b += (size_t)nT * nT * TILE_ELEMS * 8 + naux * 8;            // Kt, dq
     b += nbf_pad * naux * nocc_pad * 8;                          // X
@@ -350,6 +401,7 @@ int gdfjk_create(int device, int nbf, int naux, const unsigned char* pair_mask, 
     cudaMemset(h->d_err, 0, sizeof(int));
     h->mixed = mixed_create();
     h->oz = oz_create();
+
     if (cudaGetLastError() != cudaSuccess) {
         h->err = "create: CUDA error while initialising";
         return fail(GDFJK_ERR_CUDA);
@@ -362,7 +414,8 @@ int gdfjk_destroy(gdfjk_t h) {
     if (!h) return GDFJK_OK;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    double* bufs[] = {h->B,   h->Cl,  h->Cr,  h->D,     h->Dw,  h->dq,  h->Jt,  h->Xl, h->Xr,  h->Kpart,
+    big_free(h->B);
+    double* bufs[] = {h->Cl,  h->Cr,  h->D,     h->Dw,  h->dq,  h->Jt,  h->Xl, h->Xr,  h->Kpart,
                       h->Kt,  h->dJ,  h->dK,  h->dD,    h->dCin, h->dCrin, h->gJp, h->gKp, h->Jg, h->Yb,
                       h->Zpart, h->dCp, h->gq, h->Dw2, h->Jgt, h->hC,  h->hgJ, h->hgK, h->hdC, h->hG};
     for (double* p : bufs)
@@ -387,7 +440,7 @@ static int upload_rows_device(gdfjk_t h, const double* Bq, int q0, int nq) {
     int rc;
     if (q0 == 0) {
         if (!h->B) {
-            if ((rc = dalloc(h, &h->B, (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+            if ((rc = alloc_B(h))) return rc;
         }
         h->B_ready = false;
         mixed_invalidate(h->mixed);
@@ -443,7 +496,7 @@ int gdfjk_upload_B_device(gdfjk_t h, const double* Bq) {
     CK(cudaSetDevice(h->device));
     int rc;
     if (!h->B) {
-        if ((rc = dalloc(h, &h->B, (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+        if ((rc = alloc_B(h))) return rc;
     }
     TileLayout L = layout_of(h);
     const int chunk = 4096;
@@ -483,7 +536,7 @@ int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_sk
     CK(cudaSetDevice(h->device));
     int rc;
     if (!h->B) {
-        if ((rc = dalloc(h, &h->B, (size_t)h->naux * std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
+        if ((rc = alloc_B(h))) return rc;
     }
     const size_t nbf = h->nbf;
     const size_t npair = nbf * (nbf + 1) / 2;

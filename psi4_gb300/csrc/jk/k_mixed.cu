@@ -459,8 +459,7 @@ MixedState* mixed_create() { return new MixedState(); }
 static void free_all(MixedState* m) {
     void* ps[] = {m->Bh, m->Bl, m->Uh, m->Ul, m->Xh, m->Xl, m->part, m->Kacc, m->err, m->d_tiles, m->d_tile_of_block,
                   m->zero_blk, m->d_mb_ptr, m->d_mb_kb};
-    for (void* p : ps)
-        if (p) cudaFree(p);
+    for (void* p : ps) big_free(p);
     m->Bh = m->Bl = m->Uh = m->Ul = m->Xh = m->Xl = nullptr;
     m->part = nullptr;
     m->Kacc = nullptr;
@@ -484,8 +483,8 @@ void mixed_destroy(MixedState* m) {
 
 void mixed_invalidate(MixedState* m) {
     if (!m) return;
-    if (m->Bh) cudaFree(m->Bh);
-    if (m->Bl) cudaFree(m->Bl);
+    big_free(m->Bh);
+    big_free(m->Bl);
     m->Bh = m->Bl = nullptr;
     m->B_ready = false;
     m->have_prev = false;
@@ -501,10 +500,8 @@ size_t mixed_query_memory(int nbf, int naux, int max_nocc) {
 }
 
 static int dalloc_bytes(void** p, size_t bytes, std::string& err) {
-    if (*p) {
-        cudaFree(*p);
-        *p = nullptr;
-    }
+    big_free(*p);
+    *p = nullptr;
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();

@@ -1366,9 +1366,10 @@ int oz_alloc(void** p, size_t bytes, std::string& err) {
 }
 
 void oz_free(void** p) {
-    if (*p) cudaFree(*p);
+    big_free(*p);
     *p = nullptr;
 }
+
 
 double x_cap_bytes() {
     const char* s = getenv("GDFJK_OZ_XCAP_GB");

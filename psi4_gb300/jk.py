@@ -37,7 +37,8 @@ def _p(a):
 
 
 class DFJKEngine:
-    """Owner of one ``gdfjk_t`` handle (one device, one stream, B resident in HBM)."""
+    """Owner of one ``gdfjk_t`` handle (one device, one stream; B resident in HBM, or with
+    ``flags=abi.B_HOST`` in pinned Grace memory that the kernels read over NVLink-C2C)."""
 
     def __init__(self, nbf: int, naux: int, pair_mask: np.ndarray | None = None, device: int = 0, flags: int = 0):
         self.L = _native.jk_lib()
