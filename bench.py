@@ -879,7 +879,7 @@ def main():
     ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
                     help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
     ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
-    ap.add_argument("--host-b", default="c4",
+    ap.add_argument("--host-b", default="c4,c2",
                     help="configurations measured with B in pinned host memory (GDFJK_B_HOST), '' for none")
     args = ap.parse_args()
     if args.warmup < 3:
