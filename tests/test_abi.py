@@ -43,3 +43,13 @@ def test_create_rejects_bad_sizes_without_gpu(jk_built):
     h = ctypes.c_void_p()
     assert L.gdfjk_create(0, 0, 10, None, 0, ctypes.byref(h)) == _jkabi.GDFJK_ERR_ARG
     assert b"positive" in L.gdfjk_last_error(None)
+
+
+def test_query_memory_leaves_host_b_out_without_gpu(jk_built):
+    """With GDFJK_B_HOST the FP64 tiles of B live in host memory: the device estimate drops
+    by exactly their bytes (C2 shape, dense: 435 stored tiles)."""
+    from psi4_gb300.jk import DFJKEngine
+
+    full = DFJKEngine.query_memory(1856, 4448, 160)
+    host = DFJKEngine.query_memory(1856, 4448, 160, _jkabi.B_HOST)
+    assert full - host == 4448 * 435 * 4096 * 8
