@@ -204,6 +204,33 @@ def density_difference_factor(C_new, C_old, tol=1e-13):
     return np.ascontiguousarray(U), int((lam > 0).sum())
 
 
+def build_jk(primary, aux, molecule, options: dict | None = None, device: int = 0) -> "GpuDFJK":
+    """JK::build_JK for SCF_TYPE MEM_DF (psi4/src/psi4/libfock/jk.cc:72-160) with the options
+    that reach MemDFJK, applied as psi4 applies them:
+      SCREENING       CSAM (default), SCHWARZ or NONE: the Schwarz cutoff is INTS_TOLERANCE, or
+                      0 for NONE (jk.cc:112); DENSITY raises psi4's error unless DF_SCF_GUESS
+                      (jk.cc:83-109) — MemDFJK itself has no density screening
+      INTS_TOLERANCE  default 1e-12;  DF_FITTING_CONDITION  default 1e-10
+      SCF_SUBTYPE     AUTO, INCORE or OUT_OF_CORE: psi4's MemDFJK does not read it; here
+                      OUT_OF_CORE keeps B in Grace memory (GDFJK_B_HOST), with the same results."""
+    o = {"SCREENING": "CSAM", "INTS_TOLERANCE": DEFAULT_CUTOFF, "DF_SCF_GUESS": True, "SCF_SUBTYPE": "AUTO",
+         "DF_FITTING_CONDITION": DEFAULT_CONDITION}
+    o.update({str(k).upper(): v for k, v in (options or {}).items()})
+    screening = str(o["SCREENING"]).upper()
+    if screening not in ("SCHWARZ", "CSAM", "DENSITY", "NONE"):
+        raise ValueError(f"SCREENING must be SCHWARZ, CSAM, DENSITY or NONE, not {screening}")
+    if screening == "DENSITY" and not o["DF_SCF_GUESS"]:
+        raise RuntimeError("SCREENING=DENSITY has not been implemented for MEM_DF.")
+    subtype = str(o["SCF_SUBTYPE"]).upper()
+    if subtype not in ("AUTO", "INCORE", "OUT_OF_CORE"):
+        raise ValueError("Invalid SCF_SUBTYPE option! The choices for SCF_SUBTYPE are AUTO, INCORE, and OUT_OF_CORE.")
+    jk = GpuDFJK(primary, aux, molecule, device=device)
+    jk.set_cutoff(0.0 if screening == "NONE" else float(o["INTS_TOLERANCE"]))
+    jk.set_condition(float(o["DF_FITTING_CONDITION"]))
+    jk.set_b_host(subtype == "OUT_OF_CORE")
+    return jk
+
+
 class GpuDFJK:
     """A drop-in for psi4's MemDFJK in an RHF loop, served by the GB300 engine."""
 
@@ -220,6 +247,7 @@ class GpuDFJK:
         self.incremental = False
         self.print_level = 1
         self.engine: DFJKEngine | None = None
+        self.b_host = False  # B in pinned Grace memory (GDFJK_B_HOST)
         self._Cl, self._Cr = [], []
         self._J, self._K, self._D = [], [], []
         self.last_timings = {}
@@ -264,6 +292,11 @@ class GpuDFJK:
     def set_print(self, p):
         self.print_level = int(p)
 
+    def set_b_host(self, v: bool):
+        """Keep B in pinned host (Grace) memory, read over NVLink-C2C: results are unchanged,
+        HBM holds only the workspaces (and the tensor-core forms' derived copies)."""
+        self.b_host = bool(v)
+
     def set_precision(self, p: str):
         if p not in ("fp64", "fp64-emulated", "mixed"):
             raise ValueError("precision must be 'fp64', 'fp64-emulated' or 'mixed'")
@@ -284,6 +317,7 @@ class GpuDFJK:
         nbf = self.df.nbf if self.df is not None else self.primary.nbf
         naux = self.df.naux if self.df is not None else self.aux.nbf
         flags = {"mixed": abi.MIXED, "fp64-emulated": abi.EMULATED}.get(self.precision, 0)
+        flags |= abi.B_HOST if self.b_host else 0
         return DFJKEngine.query_memory(nbf, naux, nbf, flags) // 8
 
     def initialize(self):
@@ -293,7 +327,8 @@ class GpuDFJK:
         if self.df is None:
             self.df = build_df_tensor(self.molecule, self.primary, self.aux, self.cutoff, self.condition)
         df = self.df
-        self.engine = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask, device=self.device)
+        self.engine = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask, device=self.device,
+                                 flags=abi.B_HOST if self.b_host else 0)
         self.engine.upload_pqq(df.to_pQq(), df.sparsity)
 
     def print_header(self):

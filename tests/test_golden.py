@@ -100,3 +100,35 @@ def test_jkmemory_memdf(ints_built, basis, key):
     fun_max, shell_max = Integrals(mol, pb, pb).schwarz()
     sp = prepare_sparsity(fun_max, shell_max, 1e-12, naux)
     assert memdfjk_memory_estimate(sp, pb.nbf, naux, qmax, nthreads=1) == ref[key]
+
+
+def test_screening_none_oracle_o2(ints_built):
+    """SCREENING=NONE (cutoff 0, every function pair kept) gives the same singlet-O2 DF energy
+    as the default Schwarz cutoff (tests/pytests/test_comprehensive_jk_screening.py, MEM_DF
+    rows, 6 decimals), through the oracle JK."""
+    from psi4_gb300.dfhelper import build_df_tensor
+
+    ref = reference_values()["scf5_singlet_df"]
+    mol, pb, ab, ints, _ = system("o2", "cc-pvtz")
+    df = build_df_tensor(mol, pb, ab, cutoff=0.0, ints=ints)
+    assert df.sparsity.pair_mask.all()
+    jk = OracleJK(df.to_pQq(), df.sparsity, df.nbf, df.naux)
+    r = rhf(jk, core_hamiltonian(ints), ints.overlap(), mol.nelectron // 2, mol.nuclear_repulsion_energy(),
+            e_conv=1e-10, d_conv=1e-8)
+    assert abs(r.energy - ref["energy"]) < ref["tolerance"]
+
+
+def test_build_jk_options_without_gpu():
+    """psi4's option handling for MEM_DF (jk.cc:83-112): NONE -> cutoff 0, DENSITY raises
+    without DF_SCF_GUESS, OUT_OF_CORE selects B in Grace memory; nothing touches a GPU."""
+    from psi4_gb300.jk import build_jk
+
+    jk = build_jk(None, None, None, {"screening": "NONE"})
+    assert jk.cutoff == 0.0 and not jk.b_host
+    jk = build_jk(None, None, None, {"SCREENING": "SCHWARZ", "INTS_TOLERANCE": 1e-10, "SCF_SUBTYPE": "OUT_OF_CORE"})
+    assert jk.cutoff == 1e-10 and jk.b_host
+    assert build_jk(None, None, None, {"SCREENING": "DENSITY"}).cutoff == 1e-12  # DF_SCF_GUESS on
+    with pytest.raises(RuntimeError, match="SCREENING=DENSITY has not been implemented for MEM_DF."):
+        build_jk(None, None, None, {"SCREENING": "DENSITY", "DF_SCF_GUESS": False})
+    with pytest.raises(ValueError):
+        build_jk(None, None, None, {"SCF_SUBTYPE": "YOSHIMINE_OUT_OF_CORE"})
