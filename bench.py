@@ -386,6 +386,12 @@ def run_gpu(args):
                 out["extra_configs"][cfg] = {"unavailable": str(ex)[:300]}
             torch.cuda.empty_cache()
 
+    if rank == 0 and args.metric:
+        try:
+            out["metric_contraction"] = measure_metric(args.metric, dev, args, peaks)
+        except Exception as ex:
+            out["metric_contraction"] = {"unavailable": str(ex)[:300]}
+        torch.cuda.empty_cache()
     if rank == 0 and args.host_b:
         out["host_b"] = {}
         for cfg in [c for c in args.host_b.split(",") if c]:
@@ -529,6 +535,54 @@ def measure_config(cfg, dev, args, peaks):
     out["device_memory_in_use_gb"] = (total - free) / 1e9  # all engine buffers of both forms allocated
     eng.close()
     return out
+
+
+def measure_metric(cfg, dev, args, peaks):
+    """The metric contraction B = M (P|mn) (gdfjk_metric_contract_device, 8-digit emulated
+    FP64 on the tensor cores) at a configuration's naux x pairs: synthetic operands on the
+    device (M ~ N(0, 10^2), (P|mn) ~ N(0, 1)), the whole call timed (splits, column chunks,
+    product), and a slice of columns checked against and timed with the FP64 library GEMM."""
+    import torch
+
+    from psi4_gb300.jk import DFJKEngine
+
+    mol, nbf, naux, nocc, desc = workload_sizes(cfg)
+    npair = nbf * (nbf + 1) // 2
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(97)
+    M = torch.randn((naux, naux), dtype=torch.float64, device=dev, generator=gen) * 10.0
+    P = torch.empty((naux, npair), dtype=torch.float64, device=dev)
+    for q0 in range(0, naux, 256):
+        P[q0:min(naux, q0 + 256)].normal_(0.0, 1.0, generator=gen)
+    B = torch.empty_like(P)
+    eng = DFJKEngine(64, naux, None, device=dev.index or 0)
+    eng.metric_contract(M.data_ptr(), P.data_ptr(), 4096, B.data_ptr(), ldp=npair, ldb=npair)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.metric_contract(M.data_ptr(), P.data_ptr(), npair, B.data_ptr())
+    t = time.perf_counter() - t0
+    ncheck = min(npair, 32768)
+    (M @ P[:, :1024]).sum().item()  # the library GEMM's own first-call set-up stays out of its time
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ref = M @ P[:, :ncheck]
+    torch.cuda.synchronize()
+    t_ref = time.perf_counter() - t1
+    err = (B[:, :ncheck] - ref).abs().max().item()
+    scale = ref.abs().max().item()
+    eng.close()
+    del M, P, B, ref
+    torch.cuda.empty_cache()
+    m_p, k_p = -(-naux // 128) * 128, -(-naux // 32) * 32
+    issued = 43 * 2.0 * m_p * k_p * (-(-npair // 128) * 128)
+    sus = float(peaks.get("bf16_tflops_sustained", 1696.1))
+    return {"workload": desc + f": B = M (P|mn), naux {naux} x {npair} pairs (synthetic operands)",
+            "seconds": t, "fp64_equivalent_tflops": 2.0 * naux * naux * npair / t / 1e12,
+            "issued_bf16_tflops": issued / t / 1e12, "frac_of_sustained_bf16": issued / t / 1e12 / sus,
+            "fp64_library_gemm_s_scaled_to_all_columns": t_ref * npair / ncheck,
+            "speedup_vs_fp64_library_gemm": t_ref * npair / ncheck / t,
+            "check_columns": ncheck, "max_abs_dB_vs_fp64": err, "max_abs_B": scale,
+            "note": "43 BF16 slice-pair products per FP64 multiply-add (8 digits, levels <= 8), padded sizes"}
 
 
 def _host_mem_available():
@@ -740,6 +794,7 @@ def measure_scf_device_B(cfg, dev):
     t_gemm = time.perf_counter() - tg
     # the FP64 library GEMM on a slice of columns, for accuracy and its own rate
     ncheck = min(npair, 65536)
+    (Jm @ Pdev[:, :1024]).sum().item()  # the library GEMM's first-call set-up stays out of its time
     torch.cuda.synchronize()
     tf = time.perf_counter()
     Bref = Jm @ Pdev[:, :ncheck]
@@ -879,6 +934,7 @@ def main():
     ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
                     help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
     ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
+    ap.add_argument("--metric", default="c2", help="configuration of the metric-contraction leg, '' for none")
     ap.add_argument("--host-b", default="c4,c2",
                     help="configurations measured with B in pinned host memory (GDFJK_B_HOST), '' for none")
     args = ap.parse_args()
