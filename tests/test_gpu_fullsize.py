@@ -1,0 +1,89 @@
+"""Parity at the full (H2O)_32 cc-pVTZ size (nbf 1856, naux 4448, nocc 160; dense seeded B,
+61 GB on the device) through properties that do not need an oracle run at that size:
+the emulated-FP64 K against the native FP64 K of the same engine, linearity of J in the
+density (J(C1 | C2) = J(C1) + J(C2) for split occupied blocks), exact symmetry and bitwise
+repeatability of K, and J identical with B in Grace memory."""
+import numpy as np
+import pytest
+
+from psi4_gb300 import _jkabi as abi
+from psi4_gb300.jk import DFJKEngine
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+NBF, NAUX, NOCC = 1856, 4448, 160
+
+
+def _fill_engine(flags=0):
+    dev = torch.device("cuda:0")
+    npair = NBF * (NBF + 1) // 2
+    g = torch.Generator(device=dev)
+    g.manual_seed(4321)
+    eng = DFJKEngine(NBF, NAUX, None, flags=flags)
+    buf = torch.empty((256, npair), dtype=torch.float64, device=dev)
+    for q0 in range(0, NAUX, 256):
+        nq = min(256, NAUX - q0)
+        buf[:nq].normal_(0.0, 0.02, generator=g)
+        torch.cuda.synchronize()
+        eng.upload_device_block(buf.data_ptr(), q0, nq)
+    del buf
+    torch.cuda.empty_cache()
+    return eng
+
+
+@pytest.fixture(scope="module")
+def engine(jk_built):
+    eng = _fill_engine()
+    yield eng
+    eng.close()
+    torch.cuda.empty_cache()
+
+
+def _orbitals(seed, n=NOCC):
+    return np.random.default_rng(seed).standard_normal((NBF, n)) * 0.1
+
+
+def test_fullsize_emulated_matches_native(engine):
+    C = _orbitals(1)
+    J64, K64, _ = engine.compute(C, mode=abi.DO_J | abi.DO_K)
+    Je, Ke, _ = engine.compute(C, mode=abi.DO_J | abi.DO_K | abi.EMULATED)
+    assert np.array_equal(J64, Je)  # J is native FP64 in both
+    err = np.abs(Ke - K64).max()
+    print(f"C2 size: max|K| {np.abs(K64).max():.3e} max|dK| emulated vs native {err:.2e}")
+    assert err < 1e-10 + 1e-11 * np.abs(K64).max()
+
+
+def test_fullsize_symmetry_repeatability_and_linearity(engine):
+    C = _orbitals(2)
+    J1, K1, _ = engine.compute(C, mode=abi.DO_J | abi.DO_K | abi.EMULATED)
+    J2, K2, _ = engine.compute(C, mode=abi.DO_J | abi.DO_K | abi.EMULATED)
+    assert np.array_equal(K1, K2) and np.array_equal(J1, J2)
+    assert np.array_equal(K1, K1.T)
+    Ja, Ka, _ = engine.compute(C[:, :96], mode=abi.DO_J | abi.DO_K | abi.EMULATED)
+    Jb, Kb, _ = engine.compute(C[:, 96:], mode=abi.DO_J | abi.DO_K | abi.EMULATED)
+    dj = np.abs(Ja + Jb - J1).max()
+    dk = np.abs(Ka + Kb - K1).max()
+    print(f"C2 size: J linearity {dj:.2e} (max|J| {np.abs(J1).max():.3e}), K additivity {dk:.2e}")
+    assert dj < 1e-12 * np.abs(J1).max()
+    assert dk < 3 * (1e-10 + 1e-11 * np.abs(K1).max())  # three builds' errors
+
+
+def test_fullsize_host_b_j(engine):
+    """B in Grace memory (63 GB pinned) gives bitwise the J of the HBM-resident engine;
+    skipped when the host has less than three times that available."""
+    need = NAUX * (29 * 30 // 2) * 4096 * 8
+    avail = 0
+    with open("/proc/meminfo") as f:
+        for line in f:
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    if avail < 3 * need:
+        pytest.skip(f"{avail / 1e9:.0f} GB available host memory")
+    C = _orbitals(3)
+    J1, _, _ = engine.compute(C, mode=abi.DO_J)
+    host = _fill_engine(abi.B_HOST)
+    try:
+        J2, _, _ = host.compute(C, mode=abi.DO_J)
+    finally:
+        host.close()
+    assert np.array_equal(J1, J2)
