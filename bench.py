@@ -531,6 +531,28 @@ def measure_config(cfg, dev, args, peaks):
                                                        "note": "issued BF16 flops of measured sustained bf16"}}
     except Exception as ex:
         out["fp64_emulated"] = {"unavailable": str(ex)[:300]}
+    if nbf <= 512:  # C_left != C_right (compute_J + two-C K), emulated vs native FP64; small shapes only
+        try:
+            Cr = torch.randn((nbf, nocc), dtype=torch.float64, device=dev, generator=gen) * 0.1
+
+            def run_pair(mode, n):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(n):
+                    eng.compute_device(C.data_ptr(), Cr.data_ptr(), nocc, nocc, mode, None, J.data_ptr(), K.data_ptr())
+                e1.record(stream)
+                eng.synchronize()
+                return e0.elapsed_time(e1) / 1e3 / n
+
+            run_pair(fp, 1)
+            tn = run_pair(fp, 2)
+            run_pair(fp | abi.EMULATED, 2)
+            te2 = run_pair(fp | abi.EMULATED, max(3, args.steps))
+            out["nonsymmetric"] = {"fp64_builds_per_s": 1.0 / tn, "emulated_builds_per_s": 1.0 / te2,
+                                   "emulated_speedup": tn / te2}
+        except Exception as ex:
+            out["nonsymmetric"] = {"unavailable": str(ex)[:300]}
     free, total = torch.cuda.mem_get_info(dev)
     out["device_memory_in_use_gb"] = (total - free) / 1e9  # all engine buffers of both forms allocated
     eng.close()

@@ -53,8 +53,8 @@ enum {
     GDFJK_RESET = 16,      /* forget the incremental history (next build is a full build)      */
     GDFJK_EMULATED = 32    /* K to FP64 accuracy from BF16 tensor-core products of 7-bit digit
                               slices (Ozaki splitting, exact FP32 level sums, double-float
-                              epilogue); lr-symmetric densities, nocc <= 1024; ignored with
-                              GDFJK_MIXED                                                      */
+                              epilogue); lr-symmetric or C_left != C_right, nocc <= 1024;
+                              ignored with GDFJK_MIXED                                         */
 };
 
 /* gdfjk_create flags */

@@ -246,13 +246,15 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
             }
             if (rc) return rc;
         } else if (mode & GDFJK_EMULATED) {
-            if (nonsym) return set_err(h, GDFJK_ERR_ARG, "emulated-FP64 K needs an lr-symmetric density");
             h->last_emulated = true;
-            rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
+            const double* Cr = nonsym ? h->Cr : nullptr;
+            rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, Cr, nocc, nocc_pad, K, h->ev[3], s,
+                            h->err);
             if (rc == GDFJK_ERR_OOM) {  // give the mixed form's split copy of B back and retry once
                 CK(cudaStreamSynchronize(s));
                 mixed_invalidate(h->mixed);
-                rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, nocc, nocc_pad, K, h->ev[3], s, h->err);
+                rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, Cr, nocc, nocc_pad, K, h->ev[3], s,
+                                h->err);
             }
             if (rc) return rc;
         } else {

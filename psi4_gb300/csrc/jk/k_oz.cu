@@ -1334,6 +1334,17 @@ struct OzState {
     int* d_mb_kb = nullptr;
     int* d_blk_mb = nullptr;
     int nnz = 0, lists_nbf_p = 0;
+    // non-symmetric builds (C_left != C_right): digits of C_right and of its X, all tiles
+    int* eC_r = nullptr;
+    float* sC_r = nullptr;
+    __nv_bfloat16* Cd_r = nullptr;
+    size_t Cr_cap = 0, scr_cap = 0;
+    __nv_bfloat16* Xd_r = nullptr;
+    size_t Xr_cap = 0;
+    float* Sx_r = nullptr;
+    size_t sxr_cap = 0;
+    int2* d_tiles_all = nullptr;
+    int tiles_all_nbf_p = 0, ntiles_all = 0;
 };
 
 OzState* oz_create() { return new OzState(); }
@@ -1387,7 +1398,9 @@ void oz_release(OzState* o) {
     oz_free((void**)&o->rowmax);
     oz_free((void**)&o->Xdf);
     oz_free((void**)&o->Xd);
+    oz_free((void**)&o->Xd_r);
     o->X_cap = 0;
+    o->Xr_cap = 0;
     o->B_ready = false;
 }
 
@@ -1401,7 +1414,7 @@ void oz_destroy(OzState* o) {
     if (!o) return;
     oz_release(o);
     void* ps[] = {o->eC, o->sC, o->Cd, o->xmax, o->Sx, o->part, o->d_tiles, o->d_tob, o->err, o->d_mb_ptr, o->d_mb_kb,
-                  o->d_blk_mb};
+                  o->d_blk_mb, o->eC_r, o->sC_r, o->Cd_r, o->Sx_r, o->d_tiles_all};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (cudaEvent_t e : o->tr_ev) cudaEventDestroy(e);
@@ -1449,6 +1462,8 @@ int oz_prepare(OzState* o, cudaStream_t s, std::string& err) {
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
         cudaFuncSetAttribute(oz_contract_kernel<GM_NS, GM_NACC, GM_MAXL, GM_ASLOTS, true>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
         o->attrs_set = true;
     }
     return GDFJK_OK;
@@ -1457,7 +1472,8 @@ int oz_prepare(OzState* o, cudaStream_t s, std::string& err) {
 }  // namespace
 
 int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
-               int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s, std::string& err) {
+               const double* Crpad, int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
+               std::string& err) {
     using namespace oz;
     int rc;
     const int nbf_p = round_up(nbf, MM);
@@ -1519,15 +1535,32 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         if ((rc = oz_alloc((void**)&o->Cd, ce * 2, err))) return rc;
         o->C_cap = ce;
     }
-    oz_col_scale_kernel<<<ncols, 256, 0, s>>>(Cpad, nbf, nocc_pad, nocc, o->eC, o->sC);
-    {
+    const bool nonsym = Crpad != nullptr;
+    if (nonsym) {
+        if ((size_t)ncols > o->scr_cap) {
+            if ((rc = oz_alloc((void**)&o->eC_r, ncols * sizeof(int), err)) ||
+                (rc = oz_alloc((void**)&o->sC_r, ncols * 4, err)))
+                return rc;
+            o->scr_cap = ncols;
+        }
+        if (ce > o->Cr_cap) {
+            if ((rc = oz_alloc((void**)&o->Cd_r, ce * 2, err))) return rc;
+            o->Cr_cap = ce;
+        }
+    }
+    for (int side = 0; side < (nonsym ? 2 : 1); ++side) {
+        const double* Cs = side ? Crpad : Cpad;
+        int* eCs = side ? o->eC_r : o->eC;
+        float* sCs = side ? o->sC_r : o->sC;
+        __nv_bfloat16* Cds = side ? o->Cd_r : o->Cd;
+        oz_col_scale_kernel<<<ncols, 256, 0, s>>>(Cs, nbf, nocc_pad, nocc, eCs, sCs);
         const size_t total = (size_t)ncols * (nbf_p / 8);
         const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)o->num_sms * 8);
-        oz_split_C_kernel<<<blocks, 256, 0, s>>>(Cpad, nbf, nbf_p, nocc_pad, N, ncols, o->eC, o->Cd);
+        oz_split_C_kernel<<<blocks, 256, 0, s>>>(Cs, nbf, nbf_p, nocc_pad, N, ncols, eCs, Cds);
     }
     // ---- batches of aux functions (multiples of the group size) bounded by the X buffers
     const int G = std::max(1, RUN_K / nocc_p);
-    const double per_q = (double)nocc_p * ((double)nbf * 8.0 + (double)nbf_p * NSL * 2.0);
+    const double per_q = (double)nocc_p * ((double)nbf * 8.0 + (nonsym ? 2.0 : 1.0) * (double)nbf_p * NSL * 2.0);
     int qb = (int)std::min<double>((double)naux, std::max<double>(G, std::floor(x_cap_bytes() / per_q / G) * G));
     qb = std::max(1, qb);
     if ((size_t)qb > o->X_cap) {
@@ -1544,6 +1577,26 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     if ((size_t)nbf_p * ngroups_max > o->sx_cap) {
         if ((rc = oz_alloc((void**)&o->Sx, (size_t)nbf_p * ngroups_max * 4, err))) return rc;
         o->sx_cap = (size_t)nbf_p * ngroups_max;
+    }
+    if (nonsym) {
+        if ((size_t)qb > o->Xr_cap) {
+            if ((rc = oz_alloc((void**)&o->Xd_r, (size_t)nbf_p * qb * nocc_p * NSL * 2, err))) return rc;
+            o->Xr_cap = qb;
+        }
+        if ((size_t)nbf_p * ngroups_max > o->sxr_cap) {
+            if ((rc = oz_alloc((void**)&o->Sx_r, (size_t)nbf_p * ngroups_max * 4, err))) return rc;
+            o->sxr_cap = (size_t)nbf_p * ngroups_max;
+        }
+        // every (128-row block, 64-column block) of K, row-block-major
+        if (o->tiles_all_nbf_p != nbf_p) {
+            std::vector<int2> tl;
+            for (int I = 0; I < nmb; ++I)
+                for (int Jc = 0; Jc < nbf_p / CT_N; ++Jc) tl.push_back(make_int2(I, Jc));
+            if ((rc = oz_alloc((void**)&o->d_tiles_all, tl.size() * sizeof(int2), err))) return rc;
+            cudaMemcpy(o->d_tiles_all, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice);
+            o->ntiles_all = (int)tl.size();
+            o->tiles_all_nbf_p = nbf_p;
+        }
     }
     // ---- contraction tiles: (128-row block, 64-row block) pairs of the lower triangle
     if (o->tiles_nbf_p != nbf_p) {
@@ -1572,7 +1625,8 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         return GDFJK_ERR_ARG;
     }
     const int nbatch = (naux + qb - 1) / qb;
-    while ((int)o->tr_ev.size() < 2 * nbatch) {
+    const int nsides = nonsym ? 2 : 1;  // half-transforms per batch, each timed by an event pair
+    while ((int)o->tr_ev.size() < 2 * nsides * nbatch) {
         cudaEvent_t e;
         if (cudaEventCreate(&e) != cudaSuccess) {
             err = "emulated FP64: cudaEventCreate failed";
@@ -1580,48 +1634,81 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         }
         o->tr_ev.push_back(e);
     }
-    o->n_tr = nbatch;
+    o->n_tr = nsides * nbatch;
     for (int q0 = 0, batch = 0; q0 < naux; q0 += qb, ++batch) {
         const int nq = std::min(qb, naux - q0);
         const int ngroups = (nq + G - 1) / G;
         const size_t kdim_b = (size_t)nq * nocc_p;
         const size_t nkbt = kdim_b / MK;
-        cudaMemsetAsync(o->xmax, 0, (size_t)nbf * ngroups * 4, s);
-        TrArgs ta{};
-        ta.Bd = o->Bd;
-        ta.Cd = o->Cd;
-        ta.sA = o->sA;
-        ta.sC = o->sC;
-        ta.Xdf = o->Xdf;
-        ta.xmax = o->xmax;
-        ta.q0 = q0;
-        ta.nq = nq;
-        ta.nmb = nmb;
-        ta.nkb = nkb;
-        ta.nbf = nbf;
-        ta.nbf_p = nbf_p;
-        ta.nocc_p = nocc_p;
-        ta.N = N;
-        ta.nchunk = nchunk;
-        ta.G = G;
-        ta.ngroups = ngroups;
-        ta.kdim_b = kdim_b;
-        ta.stages = tr_stages;
-        ta.mb_ptr = o->d_mb_ptr;
-        ta.mb_kb = o->d_mb_kb;
-        ta.nnz = o->nnz;
-        ta.ncols = ncols;
-        ta.run_kb = TR_RUN_K / MK;
-        ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;
-        ta.n_items = nq * nmb * nchunk;
-        ta.err = o->err;
-        cudaEventRecord(o->tr_ev[2 * batch], s);
-        oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
-        cudaEventRecord(o->tr_ev[2 * batch + 1], s);
-        // the transform phase ends with the last batch's half-transform kernel
-        if (ev_transform_done && q0 + qb >= naux) cudaEventRecord(ev_transform_done, s);
-        oz_split_X_kernel<<<dim3((unsigned)nmb, (unsigned)ngroups), 256, 0, s>>>(
-            o->Xdf, o->xmax, nbf, nbf_p, ngroups, G, nq, nocc_p, kdim_b, nkbt, o->Sx, o->Xd);
+        for (int side = 0; side < nsides; ++side) {
+            // X = B C (side 0: C_left, 1: C_right) -> its digits and group weights
+            cudaMemsetAsync(o->xmax, 0, (size_t)nbf * ngroups * 4, s);
+            TrArgs ta{};
+            ta.Bd = o->Bd;
+            ta.Cd = side ? o->Cd_r : o->Cd;
+            ta.sA = o->sA;
+            ta.sC = side ? o->sC_r : o->sC;
+            ta.Xdf = o->Xdf;
+            ta.xmax = o->xmax;
+            ta.q0 = q0;
+            ta.nq = nq;
+            ta.nmb = nmb;
+            ta.nkb = nkb;
+            ta.nbf = nbf;
+            ta.nbf_p = nbf_p;
+            ta.nocc_p = nocc_p;
+            ta.N = N;
+            ta.nchunk = nchunk;
+            ta.G = G;
+            ta.ngroups = ngroups;
+            ta.kdim_b = kdim_b;
+            ta.stages = tr_stages;
+            ta.mb_ptr = o->d_mb_ptr;
+            ta.mb_kb = o->d_mb_kb;
+            ta.nnz = o->nnz;
+            ta.ncols = ncols;
+            ta.run_kb = TR_RUN_K / MK;
+            ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;
+            ta.n_items = nq * nmb * nchunk;
+            ta.err = o->err;
+            const int ev = 2 * (nsides * batch + side);
+            cudaEventRecord(o->tr_ev[ev], s);
+            oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
+            cudaEventRecord(o->tr_ev[ev + 1], s);
+            // the transform phase ends with the last batch's last half-transform kernel
+            if (ev_transform_done && q0 + qb >= naux && side == nsides - 1) cudaEventRecord(ev_transform_done, s);
+            oz_split_X_kernel<<<dim3((unsigned)nmb, (unsigned)ngroups), 256, 0, s>>>(
+                o->Xdf, o->xmax, nbf, nbf_p, ngroups, G, nq, nocc_p, kdim_b, nkbt, side ? o->Sx_r : o->Sx,
+                side ? o->Xd_r : o->Xd);
+        }
+        if (nonsym) {
+            // K (+)= X_left X_right^T over every tile, written straight into K (nbf x nbf)
+            CtArgs ca{};
+            ca.Xd = o->Xd;
+            ca.Yd = o->Xd_r;
+            ca.Sx = o->Sx;
+            ca.Sy = o->Sx_r;
+            ca.tiles = o->d_tiles_all;
+            ca.ntiles = o->ntiles_all;
+            ca.nsplit = 1;
+            ca.gps = ngroups;
+            ca.ngroups = ngroups;
+            ca.kpg = G * nocc_p / MK;
+            ca.nkb = (int)nkbt;
+            ca.lds_x = ca.lds_y = nbf_p;
+            ca.nkbt = nkbt;
+            ca.part = nullptr;
+            ca.out = K;
+            ca.ldo = (size_t)nbf;
+            ca.M = ca.N = nbf;
+            ca.accumulate = batch > 0 ? 1 : 0;
+            ca.stages = ct_stages;
+            ca.n_items = o->ntiles_all;
+            ca.err = o->err;
+            oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, true>
+                <<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+            continue;
+        }
         // split over groups so that there are about two work items per SM
         int nsplit = std::max(1, std::min(ngroups, (2 * o->num_sms + o->ntiles - 1) / o->ntiles));
         const int gps = (ngroups + nsplit - 1) / nsplit;

@@ -367,9 +367,9 @@ class GpuDFJK:
             mode |= abi.MIXED
             if self.incremental:
                 mode |= abi.INCREMENTAL
-        # the emulated form serves lr-symmetric densities with up to 1024 occupied columns; others
-        # take the native FP64 K
-        emu = abi.EMULATED if (self.precision == "fp64-emulated" and lr_symmetric and
+        # the emulated form serves densities with up to 1024 occupied columns (lr-symmetric or
+        # C_left != C_right); wider ones take the native FP64 K
+        emu = abi.EMULATED if (self.precision == "fp64-emulated" and
                                all(C.shape[1] <= 1024 for C in self._Cl)) else 0
         mode |= emu
         self._J, self._K, self._D = [], [], []

@@ -172,6 +172,44 @@ def test_emulated_block_sparse(jk_built):
     assert np.array_equal(Ke, Ke2)
 
 
+@pytest.mark.parametrize("case", [("h2o", "cc-pvdz"), ("h2o_2", "cc-pvdz"), ("h2o_2_far", "cc-pvdz")])
+@pytest.mark.parametrize("nocc", [16, 20, 30])
+def test_emulated_nonsymmetric_pairs(ints_built, jk_built, case, nocc):
+    """tests/pytests/test_dfjk.py style random C_left != C_right pairs: K = sum_Q (B_Q Cl)(B_Q Cr)^T
+    from two half-transforms and a contraction over every tile; J is native FP64."""
+    mol, pb, ab, ints, df = system(*case)
+    eng = _engine(df)
+    Cl = random_orbitals(df.nbf, nocc, seed=100 + nocc)
+    Cr = random_orbitals(df.nbf, nocc, seed=200 + nocc)
+    J, K, _ = eng.compute(Cl, Cr, mode=EMU)
+    J64, K64, _ = eng.compute(Cl, Cr, mode=abi.DO_J | abi.DO_K)
+    Kr = dfjk_ref.compute_K(df.to_pQq(), df.sparsity, Cl, Cr, df.nbf, df.naux, lr_symmetric=False)
+    err = np.abs(K - Kr).max()
+    print(f"{case[0]} nocc {nocc}: max|K| {np.abs(Kr).max():.3e} max|dK| {err:.2e} (native {np.abs(K64 - Kr).max():.2e})")
+    assert np.array_equal(J, J64)
+    assert err < TOL + 1e-11 * np.abs(Kr).max()
+    assert np.abs(K - K.T).max() > 0  # really non-symmetric
+
+
+def test_emulated_nonsymmetric_batches_and_jk_front_end(ints_built, jk_built, monkeypatch):
+    """Many aux batches (K accumulated over them in place) and GpuDFJK's C_left/C_right pairs
+    routed to the emulated form."""
+    df, C = _scf_orbitals("h2o_8", "cc-pvdz")
+    Cr = C + 0.01 * random_orbitals(df.nbf, C.shape[1], seed=5)
+    Kr = dfjk_ref.compute_K(df.to_pQq(), df.sparsity, C, Cr, df.nbf, df.naux, lr_symmetric=False)
+    monkeypatch.setenv("GDFJK_OZ_XCAP_GB", "0.002")
+    _, K, _ = _engine(df).compute(C, Cr, mode=EMU)
+    assert np.abs(K - Kr).max() < TOL
+    monkeypatch.delenv("GDFJK_OZ_XCAP_GB")
+    jk = GpuDFJK.from_tensor(df)
+    jk.set_precision("fp64-emulated")
+    jk.initialize()
+    jk.C_left_add(C)
+    jk.C_right_add(Cr)
+    jk.compute()
+    assert np.abs(jk.K()[0] - Kr).max() < TOL
+
+
 def test_emulated_rejects_wide_occupation(jk_built):
     """More than 1024 occupied columns would overrun one exact contraction run: refused with a
     clear error (GpuDFJK routes such densities to the native FP64 K)."""
