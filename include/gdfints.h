@@ -62,6 +62,11 @@ int gdfints_schwarz(gdfints_basis_t b, double* fun_max, double* shell_max);
 int gdfints_three_index(gdfints_basis_t aux, gdfints_basis_t prim, const unsigned char* shell_mask,
                         int p0, int p1, double* out);
 
+/* The same with the long-range operator erf(omega r)/r, omega > 0 (psi4's erf_eri 3-index
+ * integrals (Q|w|mn) of DFHelper::prepare_AO_wK_core, dfhelper.cc:589-699). */
+int gdfints_three_index_erf(gdfints_basis_t aux, gdfints_basis_t prim, const unsigned char* shell_mask,
+                            int p0, int p1, double omega, double* out);
+
 /* First derivatives, contracted with densities, for the SCF gradient (natom x 3, added
  * into grad):
  *   gdfints_overlap_grad   : sum_mn W_mn dS_mn/dx

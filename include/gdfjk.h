@@ -123,6 +123,16 @@ int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int no
 int gdfjk_compute_device(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode,
                          double* D_out, double* J, double* K);
 
+/* Long-range exchange for range-separated functionals (DFHelper::compute_wK, dfhelper.cc:3378-3438,
+ * with the tensors of DFHelper::prepare_AO_wK_core, dfhelper.cc:589-699):
+ *   wK = sum_Q (L_Q C_left)(R_Q C_right)^T,  L = J^-1 (Q|mn) on h_left, R = (Q|erf(w r)/r|mn) on
+ *   h_right (each uploaded into its own handle like B; both handles on one device, same nbf,
+ *   naux and pair mask).  C_right = NULL: lr-symmetric, and wK is symmetrised as
+ *   MemDFJK::compute_JK does (MemDFJK.cc:103-108).  mode: 0 (native FP64) or GDFJK_EMULATED.
+ *   Host buffers; uses h_left's stream and workspaces. */
+int gdfjk_compute_wK(gdfjk_t h_left, gdfjk_t h_right, const double* C_left, const double* C_right, int nocc, int ldc,
+                     int mode, double* wK);
+
 /* The precision form's incremental build (psi4's INCFOCK idea, DirectJK.cc:138-166, applied
  * to MemDFJK's exchange): J in FP64 from C (as gdfjk_compute), and
  *   K = K_prev + sum_Q B_Q (U+ U+^T - U- U-^T) B_Q

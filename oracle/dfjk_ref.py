@@ -117,6 +117,23 @@ def compute_K(Ppq, sp, C_left, C_right, nbf, naux, lr_symmetric=True):
     return K
 
 
+def compute_wK(m1Ppq, wPpq, sp, C_left, C_right, nbf, naux, lr_symmetric=True):
+    """dfhelper.cc:3378-3438 (compute_wK): T1 = transform of J^-1 (Q|mn) (m1Ppq) with C_left,
+    T2 = transform of (Q|w|mn) (wPpq) with C_right, wK = T1 T2^T over the inner dimension
+    nocc*naux; for lr-symmetric densities MemDFJK::compute_JK then hermitivitizes wK
+    (MemDFJK.cc:103-108)."""
+    nocc = C_left.shape[1]
+    wK = np.zeros((nbf, nbf))
+    if nocc == 0:
+        return wK
+    T1 = first_transform_pQq(m1Ppq, sp, C_left, nbf, naux).reshape(nbf, naux * nocc)
+    T2 = first_transform_pQq(wPpq, sp, C_left if lr_symmetric else C_right, nbf, naux).reshape(nbf, naux * nocc)
+    wK += T1 @ T2.T
+    if lr_symmetric:
+        wK = 0.5 * (wK + wK.T)
+    return wK
+
+
 class OracleJK:
     """psi4.core.JK-shaped front end over the restatement (MemDFJK semantics)."""
 

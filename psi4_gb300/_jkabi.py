@@ -17,6 +17,7 @@ SIGNATURES = {
     "gdfjk_metric_contract_device": (I, [P, P, P, I, ctypes.c_int64, P, ctypes.c_int64, I]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
+    "gdfjk_compute_wK": (I, [P, P, P, P, I, I, I, P]),
     "gdfjk_compute_incremental": (I, [P, P, I, I, P, I, I, I, I, P, P]),
     "gdfjk_backward": (I, [P, P, I, I, P, P, P, P, I]),
     "gdfjk_query_memory": (I, [I, I, I, I, ctypes.POINTER(SZ)]),

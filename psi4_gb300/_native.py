@@ -131,6 +131,7 @@ def _declare_ints(L):
         ("gdfints_metric", [P, P]),
         ("gdfints_schwarz", [P, P, P]),
         ("gdfints_three_index", [P, P, P, I, I, P]),
+        ("gdfints_three_index_erf", [P, P, P, I, I, D, P]),
         ("gdfints_overlap_grad", [P, P, I, P]),
         ("gdfints_kinetic_grad", [P, P, I, P]),
         ("gdfints_potential_grad", [P, P, I, P, P, P]),

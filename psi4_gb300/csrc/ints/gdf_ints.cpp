@@ -389,8 +389,12 @@ struct Scratch {
 // Contracted Cartesian (AB|CD) (bra pair AB, ket pair CD; B/D may be unit shells).
 // out[ab*ncd + cd].  When deriv != 0 also fills dout[9][ab*ncd+cd]: derivatives with respect
 // to A_xyz (0-2), B_xyz (3-5), C_xyz (6-8); the D centre follows by translation invariance.
+// omega > 0: the long-range operator erf(omega r)/r instead of 1/r (psi4's erf_eri, used for
+// wK): the reduced exponent alpha of each primitive quartet becomes
+// alpha_w = alpha omega^2 / (alpha + omega^2) in the Boys argument and the Hermite recursion,
+// and the prefactor gains sqrt(alpha_w / alpha)  (erf(wr)/r = 2/sqrt(pi) int_0^w exp(-t^2 r^2) dt).
 void eri_cart(const Shell& A, const Shell& B, const Shell& C, const Shell& D, Scratch& s, double* out, int deriv,
-              double* dout) {
+              double* dout, double omega = 0.0) {
     int la = A.l, lb = B.l, lc = C.l, ld = D.l;
     int nab = ncart(la) * ncart(lb), ncd = ncart(lc) * ncart(ld);
     int Lb = la + lb + deriv, Lk = lc + ld + deriv;
@@ -444,6 +448,11 @@ void eri_cart(const Shell& A, const Shell& B, const Shell& C, const Shell& D, Sc
                     }
                     double pref = pi52 / (p * q * std::sqrt(p + q)) * cab * C.c[pc] * D.c[pd];
                     double alpha = p * q / (p + q);
+                    if (omega > 0.0) {
+                        const double aw = alpha * omega * omega / (alpha + omega * omega);
+                        pref *= std::sqrt(aw / alpha);
+                        alpha = aw;
+                    }
                     hermite_R(L, alpha, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2], s.R.data(), s.W.data());
                     // ket Hermite matrix with (-1)^{tau+nu+phi}
                     hermite_matrix(lc, ld, c, dd, Ecd, 0, Lk, s.Hk.data());
@@ -849,8 +858,11 @@ int gdfints_schwarz(gdfints_basis_t bp, double* fun_max, double* shell_max) {
     return 0;
 }
 
-int gdfints_three_index(gdfints_basis_t auxp, gdfints_basis_t primp, const unsigned char* shell_mask, int p0, int p1,
-                        double* out) {
+}  // extern "C"
+
+namespace {
+int three_index_impl(gdfints_basis_t auxp, gdfints_basis_t primp, const unsigned char* shell_mask, int p0, int p1,
+                     double omega, double* out) {
     const Basis& aux = *auxp;
     const Basis& pb = *primp;
     int nsp = static_cast<int>(pb.sh.size());
@@ -883,7 +895,7 @@ int gdfints_three_index(gdfints_basis_t auxp, gdfints_basis_t primp, const unsig
                 if (sig) {
                     Shell uC = unit_shell(C.O);
                     blk.resize(static_cast<size_t>(A.ncart) * B.ncart * C.ncart);
-                    eri_cart(A, B, C, uC, s, blk.data(), 0, nullptr);
+                    eri_cart(A, B, C, uC, s, blk.data(), 0, nullptr, omega);
                     int ls[3] = {A.l, B.l, C.l};
                     int pf[3] = {pb.puream, pb.puream, aux.puream};
                     finish_block(ls, pf, 3, blk, tmp);
@@ -903,6 +915,20 @@ int gdfints_three_index(gdfints_basis_t auxp, gdfints_basis_t primp, const unsig
         }
     }
     return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int gdfints_three_index(gdfints_basis_t auxp, gdfints_basis_t primp, const unsigned char* shell_mask, int p0, int p1,
+                        double* out) {
+    return three_index_impl(auxp, primp, shell_mask, p0, p1, 0.0, out);
+}
+
+int gdfints_three_index_erf(gdfints_basis_t auxp, gdfints_basis_t primp, const unsigned char* shell_mask, int p0, int p1,
+                            double omega, double* out) {
+    if (!(omega > 0.0)) return fail("three_index_erf: omega must be positive");
+    return three_index_impl(auxp, primp, shell_mask, p0, p1, omega, out);
 }
 
 // ------------------------------------------------------------------ gradients

@@ -659,6 +659,72 @@ int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int no
     return check_device_flag(h);
 }
 
+int gdfjk_compute_wK(gdfjk_t hl, gdfjk_t hr, const double* C_left, const double* C_right, int nocc, int ldc, int mode,
+                     double* wK) {
+    if (!hl || !hr || !wK) return set_err(hl, GDFJK_ERR_ARG, "compute_wK: null handle or output");
+    if (hl->nbf != hr->nbf || hl->naux != hr->naux || hl->map != hr->map || hl->device != hr->device)
+        return set_err(hl, GDFJK_ERR_ARG, "compute_wK: the two handles must share nbf, naux, the pair mask and the device");
+    if (!hl->B_ready || !hr->B_ready) return set_err(hl, GDFJK_ERR_STATE, "compute_wK: upload both tensors first");
+    if (nocc < 0 || (nocc > 0 && (!C_left || ldc < nocc))) return set_err(hl, GDFJK_ERR_ARG, "compute_wK: bad C / nocc / ldc");
+    gdfjk_t h = hl;  // workspaces and stream of the left handle
+    CK(cudaSetDevice(h->device));
+    int rc;
+    const size_t n2 = (size_t)h->nbf * h->nbf;
+    const size_t cin = (size_t)h->nbf * std::max(ldc, 1);
+    if (!h->dJ) {
+        if ((rc = dalloc(h, &h->dJ, n2))) return rc;
+        if ((rc = dalloc(h, &h->dK, n2))) return rc;
+        if ((rc = dalloc(h, &h->dD, n2))) return rc;
+    }
+    if (cin > h->dCin_elems) {
+        if ((rc = dalloc(h, &h->dCin, cin))) return rc;
+        if ((rc = dalloc(h, &h->dCrin, cin))) return rc;
+        h->dCin_elems = cin;
+    }
+    cudaStream_t s = h->stream;
+    if (nocc == 0) {
+        std::fill(wK, wK + n2, 0.0);
+        return GDFJK_OK;
+    }
+    const bool lr = C_right == nullptr;
+    CK(cudaMemcpyAsync(h->dCin, C_left, cin * 8, cudaMemcpyHostToDevice, s));
+    if (!lr) CK(cudaMemcpyAsync(h->dCrin, C_right, cin * 8, cudaMemcpyHostToDevice, s));
+    const int nocc_pad = round_up(nocc, 32);
+    const bool emulated = (mode & GDFJK_EMULATED) != 0;
+    if ((rc = ensure_workspace(h, nocc_pad, true, !emulated))) return rc;
+    launch_pad_C(h->dCin, h->nbf, nocc, ldc, h->nbf_pad, nocc_pad, h->Cl, s);
+    launch_pad_C(lr ? h->dCin : h->dCrin, h->nbf, nocc, ldc, h->nbf_pad, nocc_pad, h->Cr, s);
+    TileLayout L = layout_of(h), Lr = layout_of(hr);
+    if (emulated) {
+        h->last_emulated = true;
+        rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, h->Cr, nocc, nocc_pad, h->dK, nullptr, s,
+                        h->err, hr->oz, hr->B, &Lr);
+        if (rc) return set_err(h, rc, h->err);
+    } else {
+        h->last_emulated = false;
+        launch_k_transform_fp64(h->B, h->Cl, h->naux, h->nbf_pad, nocc_pad, L, h->Xl, s);
+        launch_k_transform_fp64(hr->B, h->Cr, h->naux, h->nbf_pad, nocc_pad, Lr, h->Xr, s);
+        const size_t kdim = (size_t)h->naux * nocc_pad;
+        const int ns = k_contract_splits(h->nbf_pad, kdim, false);
+        launch_k_contract_fp64(h->Xl, h->Xr, h->nbf_pad, kdim, false, L, h->Kpart, ns, h->Kt, s);
+        launch_unpack_tiles(h->Kt, L, h->nbf, h->nbf_pad, h->dK, h->nbf, false, s);
+    }
+    launch_finite_check(h->dK, n2, h->d_err, s);
+    CK(cudaMemcpyAsync(wK, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if ((rc = wait_stream(h, env_timeout()))) return rc;
+    if ((rc = check_device_flag(h))) return rc;
+    if (lr) {  // MemDFJK::compute_JK hermitivitizes wK for lr-symmetric densities (MemDFJK.cc:103-108)
+        const size_t n = (size_t)h->nbf;
+        for (size_t m = 0; m < n; ++m)
+            for (size_t k = 0; k < m; ++k) {
+                const double v = 0.5 * (wK[m * n + k] + wK[k * n + m]);
+                wK[m * n + k] = v;
+                wK[k * n + m] = v;
+            }
+    }
+    return GDFJK_OK;
+}
+
 int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
                               int mode, double* J, double* K) {
     if (!h) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: null handle");

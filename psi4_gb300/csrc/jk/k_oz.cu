@@ -1471,13 +1471,13 @@ int oz_prepare(OzState* o, cudaStream_t s, std::string& err) {
 
 }  // namespace
 
-int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
-               const double* Crpad, int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
-               std::string& err) {
+// The digit copy of B on `o` (once per upload): the (row block, k block) pairs of B that touch
+// a stored tile, then the int8 digit fields of those blocks.
+static int oz_ensure_digits(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux,
+                            cudaStream_t s, std::string& err) {
     using namespace oz;
     int rc;
     const int nbf_p = round_up(nbf, MM);
-    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
     if ((rc = oz_prepare(o, s, err))) return rc;
     // ---- the (row block, k block) pairs of B that touch a stored tile (the tile map is fixed)
     if (o->lists_nbf_p != nbf_p) {
@@ -1513,6 +1513,21 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
             B, nbf, L.nT, L.ntiles, L.map, nbf_p, o->nnz, o->d_blk_mb, o->d_mb_kb, o->d_mb_ptr, o->rowmax, o->sA, o->Bd);
         o->nbf_p = nbf_p;
         o->B_ready = true;
+    }
+    return GDFJK_OK;
+}
+
+int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
+               const double* Crpad, int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
+               std::string& err, OzState* o_right, const double* B_right, const TileLayout* L_right) {
+    using namespace oz;
+    int rc;
+    const int nbf_p = round_up(nbf, MM);
+    const int nmb = nbf_p / MM, nkb = nbf_p / MK;
+    if ((rc = oz_ensure_digits(o, B, L, map_host, nbf, naux, s, err))) return rc;
+    if (o_right) {  // K from two tensors: C_right's half-transform reads the other digit copy
+        if ((rc = oz_ensure_digits(o_right, B_right, *L_right, map_host, nbf, naux, s, err))) return rc;
+        if (!Crpad) Crpad = Cpad;
     }
     if (nocc_pad > RUN_K) {
         // one aux function's columns must fit one exact contraction run (levels 0-3 provably exact)
@@ -1643,10 +1658,11 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         for (int side = 0; side < nsides; ++side) {
             // X = B C (side 0: C_left, 1: C_right) -> its digits and group weights
             cudaMemsetAsync(o->xmax, 0, (size_t)nbf * ngroups * 4, s);
+            const OzState* ob = (side && o_right) ? o_right : o;  // digits of the tensor this side reads
             TrArgs ta{};
-            ta.Bd = o->Bd;
+            ta.Bd = ob->Bd;
             ta.Cd = side ? o->Cd_r : o->Cd;
-            ta.sA = o->sA;
+            ta.sA = ob->sA;
             ta.sC = side ? o->sC_r : o->sC;
             ta.Xdf = o->Xdf;
             ta.xmax = o->xmax;
@@ -1663,9 +1679,9 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
             ta.ngroups = ngroups;
             ta.kdim_b = kdim_b;
             ta.stages = tr_stages;
-            ta.mb_ptr = o->d_mb_ptr;
-            ta.mb_kb = o->d_mb_kb;
-            ta.nnz = o->nnz;
+            ta.mb_ptr = ob->d_mb_ptr;
+            ta.mb_kb = ob->d_mb_kb;
+            ta.nnz = ob->nnz;
             ta.ncols = ncols;
             ta.run_kb = TR_RUN_K / MK;
             ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;

@@ -20,10 +20,12 @@ size_t oz_query_memory(int nbf, int naux, int max_nocc);
 // K (nbf x nbf, device) = sum_Q (B_Q C_left)(B_Q C_right)^T (C device, nbf_pad x nocc_pad,
 // row-major; Crpad = nullptr for the lr-symmetric C C^T); records `ev_transform_done` after
 // the last half-transform.  map_host: the tile map of L on the host (digits of B are kept
-// only where a stored tile is).
+// only where a stored tile is).  With o_right, the right factor uses a second tensor
+// (B_right, same tile map, its digits kept on o_right): sum_Q (B_Q C_left)(B'_Q C_right)^T.
 int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_host, int nbf, int naux, const double* Cpad,
                const double* Crpad, int nocc, int nocc_pad, double* K, cudaEvent_t ev_transform_done, cudaStream_t s,
-               std::string& err);
+               std::string& err, OzState* o_right = nullptr, const double* B_right = nullptr,
+               const TileLayout* L_right = nullptr);
 // Summed device time (ms) of the half-transform kernels of the last build (all batches);
 // valid once that build has completed.
 float oz_last_transform_ms(OzState* o);

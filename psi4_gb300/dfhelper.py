@@ -149,3 +149,24 @@ def build_df_tensor(mol: Molecule, primary: BasisSet, aux: BasisSet, cutoff: flo
     Jm = metric_power(M, -0.5, condition)
     B = Jm @ A
     return DFTensor(primary.nbf, aux.nbf, B, sp, M, Jm)
+
+
+def build_wk_tensors(df: DFTensor, ints: Integrals, omega: float,
+                     condition: float = DEFAULT_CONDITION) -> tuple[DFTensor, DFTensor]:
+    """The two tensors of psi4's wK (DFHelper::prepare_AO_wK_core, dfhelper.cc:589-699, with
+    MemDFJK's default wcombine = false): J^-1 (Q|mn) (metric power -1.0, dfhelper.h:357, same
+    fitting condition) and the raw long-range integrals (Q|erf(w r)/r|mn), both over the
+    Schwarz sparsity of `df` (screened pairs zero).  Returned as DF tensors sharing `df`'s
+    tables, ready for an engine upload."""
+    import dataclasses
+
+    sp = df.sparsity
+    r, c = np.tril_indices(df.nbf)
+    screened = ~sp.pair_mask[r, c]
+    A = ints.three_index(shell_mask=sp.shell_mask)
+    A[:, screened] = 0.0
+    Jinv = metric_power(df.metric, -1.0, condition)
+    W = ints.three_index_erf(omega, shell_mask=sp.shell_mask)
+    W[:, screened] = 0.0
+    return dataclasses.replace(df, B_tri=Jinv @ A), dataclasses.replace(df, B_tri=W)
+

@@ -109,6 +109,20 @@ class Integrals:
         )
         return out
 
+    def three_index_erf(self, omega: float, shell_mask: np.ndarray | None = None, p0: int = 0, p1: int | None = None):
+        """(P|erf(omega r)/r|mn), the long-range 3-index integrals of psi4's wK
+        (DFHelper::prepare_AO_wK_core, dfhelper.cc:589-699), same layout as three_index."""
+        n = self.nb.nbf
+        p1 = self.na.nbf if p1 is None else p1
+        out = np.zeros((p1 - p0, n * (n + 1) // 2))
+        mask = None if shell_mask is None else np.ascontiguousarray(shell_mask, dtype=np.uint8)
+        _check(
+            self.L.gdfints_three_index_erf(self.na.h, self.nb.h, None if mask is None else _ptr(mask), p0, p1,
+                                           float(omega), _ptr(out)),
+            self.L,
+        )
+        return out
+
     # ---- gradients (natom x 3)
     def _g(self):
         return np.zeros((self.mol.natom, 3))

@@ -119,6 +119,19 @@ class DFJKEngine:
                                          nocc, max(nocc, 1), mode, _p(D), _p(J), _p(K)))
         return J, K, D
 
+    def compute_wK(self, right: "DFJKEngine", C_left, C_right=None, mode=0):
+        """wK = sum_Q (L_Q C_left)(R_Q C_right)^T with L = this engine's tensor (J^-1 (Q|mn)) and
+        R = `right`'s ((Q|w|mn)); C_right None: lr-symmetric, symmetrised like MemDFJK.
+        mode: 0 (native FP64) or abi.EMULATED."""
+        Cl = np.ascontiguousarray(C_left, dtype=np.float64)
+        Cr = None if C_right is None else np.ascontiguousarray(C_right, dtype=np.float64)
+        nocc = Cl.shape[1]
+        wK = np.empty((self.nbf, self.nbf))
+        self._check(self.L.gdfjk_compute_wK(self.h, right.h, _p(Cl) if nocc else None,
+                                            _p(Cr) if (Cr is not None and nocc) else None, nocc, max(nocc, 1),
+                                            int(mode), _p(wK)))
+        return wK
+
     def compute_incremental(self, C, U, npos, mode=abi.DO_J | abi.DO_K | abi.MIXED, reset=False):
         """Precision form: J (FP64) from C; K = K_prev + sum_Q B_Q (U+U+^T - U-U-^T) B_Q in
         split BF16 with FP32 accumulation (K_prev = 0 when reset).  Without MIXED in mode,
@@ -248,6 +261,10 @@ class GpuDFJK:
         self.print_level = 1
         self.engine: DFJKEngine | None = None
         self.b_host = False  # B in pinned Grace memory (GDFJK_B_HOST)
+        self.do_wK = False
+        self.omega = 0.0
+        self.wk_engines: tuple[DFJKEngine, DFJKEngine] | None = None
+        self._wK = []
         self._Cl, self._Cr = [], []
         self._J, self._K, self._D = [], [], []
         self.last_timings = {}
@@ -292,6 +309,16 @@ class GpuDFJK:
     def set_print(self, p):
         self.print_level = int(p)
 
+    def set_do_wK(self, v: bool):
+        """Also build the long-range exchange wK (MemDFJK with do_wK, DFHelper::compute_wK)."""
+        self.do_wK = bool(v)
+
+    def set_omega(self, w: float):
+        self.omega = float(w)
+
+    def wK(self):
+        return self._wK
+
     def set_b_host(self, v: bool):
         """Keep B in pinned host (Grace) memory, read over NVLink-C2C: results are unchanged,
         HBM holds only the workspaces (and the tensor-core forms' derived copies)."""
@@ -330,6 +357,21 @@ class GpuDFJK:
         self.engine = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask, device=self.device,
                                  flags=abi.B_HOST if self.b_host else 0)
         self.engine.upload_pqq(df.to_pQq(), df.sparsity)
+        if self.do_wK:
+            # prepare_AO_wK_core: J^-1 (Q|mn) and (Q|w|mn), one engine each
+            if self.molecule is None or not self.omega > 0:
+                raise GdfjkError(abi.GDFJK_ERR_STATE, "JK: wK needs the molecule and omega > 0")
+            from .dfhelper import build_wk_tensors
+            from .ints import Integrals
+
+            m1, w = build_wk_tensors(df, Integrals(self.molecule, self.primary, self.aux), self.omega, self.condition)
+            engines = []
+            for t in (m1, w):
+                e = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask, device=self.device,
+                               flags=abi.B_HOST if self.b_host else 0)
+                e.upload_qtri(t.B_tri)
+                engines.append(e)
+            self.wk_engines = (engines[0], engines[1])
 
     def print_header(self):
         if self.print_level:
@@ -373,6 +415,13 @@ class GpuDFJK:
                                all(C.shape[1] <= 1024 for C in self._Cl)) else 0
         mode |= emu
         self._J, self._K, self._D = [], [], []
+        self._wK = []
+        if self.do_wK and self.wk_engines is not None:
+            # DFHelper::compute_wK for every density (native FP64, or the emulated form with it)
+            left, right = self.wk_engines
+            for i, Cl in enumerate(self._Cl):
+                Cr = None if lr_symmetric else self._Cr[i]
+                self._wK.append(left.compute_wK(right, Cl, Cr, mode=emu))
         if self.precision in ("fp64", "fp64-emulated") and self.incremental and lr_symmetric and self.do_K and \
                 len(self._Cl) == 1:
             # FP64 re-anchor of the precision form: full FP64 K, kept as the incremental base

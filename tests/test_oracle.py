@@ -77,3 +77,32 @@ def test_oracle_jk_object(ints_built):
     assert np.abs(jk.J()[0] - Jd).max() < 1e-11
     assert np.abs(jk.K()[0] - Kd).max() < 1e-11
     assert np.abs(jk.D()[0] - C @ C.T).max() < 1e-14
+
+
+def test_oracle_wk_against_dense(ints_built):
+    """compute_wK (DFHelper's loop over its pQq layout) against a dense restatement with
+    full square tensors: wK = sum_Q (M1_Q C_l)(W_Q C_r)^T, hermitivitized when lr-symmetric."""
+    from oracle import dfjk_ref
+    from psi4_gb300.dfhelper import build_wk_tensors
+    from tests.helpers import random_orbitals, system
+
+    mol, pb, ab, ints, df = system("h2o", "cc-pvdz")
+    m1, w = build_wk_tensors(df, ints, 0.4)
+    nbf, naux = df.nbf, df.naux
+    r, c = np.tril_indices(nbf)
+
+    def square(tri):
+        full = np.zeros((naux, nbf, nbf))
+        full[:, r, c] = tri
+        full[:, c, r] = tri
+        return full
+
+    M1, W = square(m1.B_tri), square(w.B_tri)
+    Cl = random_orbitals(nbf, 5, seed=1)
+    Cr = random_orbitals(nbf, 5, seed=2)
+    dense = np.einsum("qmn,ni,qlk,ki->ml", M1, Cl, W, Cr)
+    got = dfjk_ref.compute_wK(m1.to_pQq(), w.to_pQq(), df.sparsity, Cl, Cr, nbf, naux, lr_symmetric=False)
+    assert np.abs(got - dense).max() < 1e-12 * max(1.0, np.abs(dense).max())
+    sym = np.einsum("qmn,ni,qlk,ki->ml", M1, Cl, W, Cl)
+    got = dfjk_ref.compute_wK(m1.to_pQq(), w.to_pQq(), df.sparsity, Cl, None, nbf, naux)
+    assert np.abs(got - 0.5 * (sym + sym.T)).max() < 1e-12 * max(1.0, np.abs(sym).max())
