@@ -468,11 +468,12 @@ __device__ __forceinline__ void issue_slice_j(int j, const uint32_t* d, uint32_t
     }
 }
 
-// The contraction's form with NS digits and levels up to MAXL: slice J against B slices
-// t <= min(NS - 1, MAXL - J), accumulator min(J + t, NA - 1).
+// The contraction's MMAs with NS digits and levels up to MAXL: A slice J (shared-memory
+// descriptor dA; 16 k = 2 descriptor units) against B slices t <= min(NS - 1, MAXL - J),
+// accumulator min(J + t, NA - 1)
 template <int NS, int NA, int MAXL, int J>
-__device__ __forceinline__ void issue_slice_g(const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step, uint32_t id,
-                                              bool first) {
+__device__ __forceinline__ void issue_slice_gs(const uint32_t* d, uint64_t dA, uint64_t dB, uint64_t b_step, uint32_t id,
+                                               bool first) {
     constexpr int TMAX = (NS - 1) < (MAXL - J) ? (NS - 1) : (MAXL - J);
 #pragma unroll
     for (int ks = 0; ks < MK / 16; ++ks) {
@@ -480,23 +481,22 @@ __device__ __forceinline__ void issue_slice_g(const uint32_t* d, uint32_t a_col,
         for (int t = 0; t <= TMAX; ++t) {
             const int L = J + t < NA - 1 ? J + t : NA - 1;
             const uint32_t f = (first && ks == 0 && J == 0 && t <= NA - 1) ? 0u : 1u;
-            mma_bf16_ta(d[L], a_col + (uint32_t)(8 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
+            tc::mma_bf16(d[L], dA + (uint64_t)(2 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
         }
     }
 }
 template <int NS, int NA, int MAXL>
-__device__ __forceinline__ void issue_slice_gj(int j, const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step,
-                                               uint32_t id, bool first) {
-    static_assert(NS <= 8 && MAXL >= NS - 1, "up to eight digits, every slice used");
+__device__ __forceinline__ void issue_slice_gjs(int j, const uint32_t* d, uint64_t dA, uint64_t dB, uint64_t b_step,
+                                                uint32_t id, bool first) {
     switch (j) {
-        case 0: issue_slice_g<NS, NA, MAXL, 0>(d, a_col, dB, b_step, id, first); break;
-        case 1: issue_slice_g<NS, NA, MAXL, 1>(d, a_col, dB, b_step, id, first); break;
-        case 2: issue_slice_g<NS, NA, MAXL, 2>(d, a_col, dB, b_step, id, first); break;
-        case 3: issue_slice_g<NS, NA, MAXL, 3>(d, a_col, dB, b_step, id, first); break;
-        case 4: issue_slice_g<NS, NA, MAXL, 4>(d, a_col, dB, b_step, id, first); break;
-        case 5: issue_slice_g<NS, NA, MAXL, 5>(d, a_col, dB, b_step, id, first); break;
-        case 6: issue_slice_g<NS, NA, MAXL, 6>(d, a_col, dB, b_step, id, first); break;
-        default: issue_slice_g<NS, NA, MAXL, (NS > 7 ? 7 : 6)>(d, a_col, dB, b_step, id, first); break;
+        case 0: issue_slice_gs<NS, NA, MAXL, 0>(d, dA, dB, b_step, id, first); break;
+        case 1: issue_slice_gs<NS, NA, MAXL, 1>(d, dA, dB, b_step, id, first); break;
+        case 2: issue_slice_gs<NS, NA, MAXL, 2>(d, dA, dB, b_step, id, first); break;
+        case 3: issue_slice_gs<NS, NA, MAXL, 3>(d, dA, dB, b_step, id, first); break;
+        case 4: issue_slice_gs<NS, NA, MAXL, 4>(d, dA, dB, b_step, id, first); break;
+        case 5: issue_slice_gs<NS, NA, MAXL, 5>(d, dA, dB, b_step, id, first); break;
+        case 6: issue_slice_gs<NS, NA, MAXL, 6>(d, dA, dB, b_step, id, first); break;
+        default: issue_slice_gs<NS, NA, MAXL, (NS > 7 ? 7 : 6)>(d, dA, dB, b_step, id, first); break;
     }
 }
 
@@ -868,18 +868,17 @@ struct CtArgs {
     int* err;
 };
 
-// Stage per k block: [NS A slices, 128 rows | NS B slices, 64 rows].  The copier warps move
-// each A slice into a TMEM slot (the MMAs take A from tensor memory and only B from shared
-// memory).  K = X X^T: 7 digits, six accumulators (levels 0-4 exact, tail 5-6) at TMEM columns
-// 0..383, seven A slots at 400..511.  The general product (metric contraction): 8 digits,
-// levels <= 8, seven accumulators (levels 0-5 exact, tail 6-8) at 0..447, four A slots.
+// Stage per k block: [NS A slices, 128 rows | NS B slices, 64 rows], both read by the MMAs
+// straight from shared memory (64-byte swizzled, K-major).  K = X X^T: 7 digits, six
+// accumulators (levels 0-4 exact, tail 5-6) at TMEM columns 0..383.  The general product
+// (metric contraction): 8 digits, levels <= 8, seven accumulators (levels 0-5 exact, tail 6-8)
+// at 0..447.
 constexpr int CT_NACC = NACC;
-constexpr int CT_ASLOTS = 7;
-constexpr int CT_THREADS = 448;  // producer, MMA, 8 epilogue warps, 4 copier warps
+constexpr int CT_THREADS = 320;  // producer, MMA, 8 epilogue warps
 __host__ __device__ constexpr int ct_stage_bytes(int ns) { return ns * BF_SLICE + ns * CT_N * MK * 2; }
 constexpr int CT_STAGE = ct_stage_bytes(NSL);  // 84 KB
-constexpr int GM_NS = 8, GM_NACC = 7, GM_MAXL = 8, GM_ASLOTS = 4;
-static_assert(GM_NACC * CT_N + GM_ASLOTS * 16 <= 512 && CT_NACC * CT_N + CT_ASLOTS * 16 <= 512, "TMEM columns");
+constexpr int GM_NS = 8, GM_NACC = 7, GM_MAXL = 8;
+static_assert(GM_NACC * CT_N <= 512 && CT_NACC * CT_N <= 512, "TMEM columns");
 
 __device__ __forceinline__ void ct_item(const CtArgs& a, int item, int& tile, int& g0, int& g1) {
     const int split = item / a.ntiles;  // split-major: concurrent CTAs share one k window in L2
@@ -890,19 +889,16 @@ __device__ __forceinline__ void ct_item(const CtArgs& a, int item, int& tile, in
 __device__ __forceinline__ int ct_kb0(const CtArgs& a, int g) { return g * a.kpg; }
 __device__ __forceinline__ int ct_kb1(const CtArgs& a, int g) { return min(a.nkb, (g + 1) * a.kpg); }
 
-template <int NS, int NA, int MAXL, int ASLOTS, bool DIRECT>
+template <int NS, int NA, int MAXL, bool DIRECT>
 __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs a) {
     constexpr int OFF_B = NS * BF_SLICE;
     constexpr int STAGE = ct_stage_bytes(NS);
-    constexpr int ACOL0 = 512 - ASLOTS * 16;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)a.stages * STAGE);
     uint64_t* empty = full + a.stages;
-    uint64_t* afull = empty + a.stages;    // [ASLOTS]
-    uint64_t* aempty = afull + ASLOTS;  // [ASLOTS]
-    uint64_t* tfull = aempty + ASLOTS;  // [2]
-    uint64_t* tempty = tfull + 2;          // [2]
+    uint64_t* tfull = empty + a.stages;  // [2]
+    uint64_t* tempty = tfull + 2;        // [2]
     uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tempty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
     const int warp = threadIdx.x / 32;
@@ -910,10 +906,6 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
         for (int s = 0; s < a.stages; ++s) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
-        }
-        for (int r = 0; r < ASLOTS; ++r) {
-            tc::mbar_init(&afull[r], 128);
-            tc::mbar_init(&aempty[r], 1);
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&tfull[b], 1);
@@ -961,72 +953,11 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                 }
             }
         }
-    } else if (warp >= 6 && warp < 10) {
-        // ---- copiers: row `row` of each A slice (swizzled BF16 in the stage) into a TMEM slot,
-        // two slices per step
-        const int q = warp % 4;
-        const int row = q * 32 + (threadIdx.x % 32);
-        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-        int s = 0, r = 0;
-        uint32_t ph = 0, pr = 0;
-        long used = 0;
-        bool ok = true;
-        for (int item = blockIdx.x; ok && item < a.n_items; item += gridDim.x) {
-            int tile, g0, g1;
-            ct_item(a, item, tile, g0, g1);
-            for (int g = g0; ok && g < g1; ++g) {
-                const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
-                for (int kb = kb0; ok && kb < kb1; ++kb) {
-                    if (!tc::mbar_wait(&full[s], ph, abort_flag, a.err)) {
-                        ok = false;
-                        break;
-                    }
-                    const uint8_t* st = smem + (size_t)s * STAGE;
-#pragma unroll 1
-                    for (int j0 = 0; ok && j0 < NS; j0 += 2) {
-                        const int nj = NS - j0 < 2 ? NS - j0 : 2;
-                        int slot[2] = {0, 0};
-                        for (int jj = 0; jj < nj; ++jj, ++used) {
-                            if (used >= ASLOTS && !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
-                                ok = false;
-                                break;
-                            }
-                            slot[jj] = r;
-                            if (++r == ASLOTS) {
-                                r = 0;
-                                pr ^= 1u;
-                            }
-                        }
-                        if (!ok) break;
-                        tc::tc_fence_after();
-                        for (int jj = 0; jj < nj; ++jj) {
-                            const uint8_t* src = st + (j0 + jj) * BF_SLICE;
-                            uint32_t o[16];
-#pragma unroll
-                            for (int c = 0; c < 4; ++c) {
-                                const uint4 v = *reinterpret_cast<const uint4*>(src + tc::swz_offset((uint32_t)row, (uint32_t)c));
-                                o[4 * c] = v.x;
-                                o[4 * c + 1] = v.y;
-                                o[4 * c + 2] = v.z;
-                                o[4 * c + 3] = v.w;
-                            }
-                            tmem_st16(lane_base + (uint32_t)(ACOL0 + 16 * slot[jj]), o);
-                        }
-                        tmem_wait_st();
-                        tc::tc_fence_before();
-                        for (int jj = 0; jj < nj; ++jj) tc::mbar_arrive(&afull[slot[jj]]);
-                    }
-                    if (++s == a.stages) {
-                        s = 0;
-                        ph ^= 1u;
-                    }
-                }
-            }
-        }
     } else if (threadIdx.x == 32) {
-        // ---- MMA issuer: per group one accumulation run; per k block seven A slices from TMEM
-        int s = 0, r = 0;
-        uint32_t ph = 0, pr = 0;
+        // ---- MMA issuer: per group one accumulation run; per k block every A slice against
+        // the B slices of its levels, both operands from the stage
+        int s = 0;
+        uint32_t ph = 0;
         int gi = 0;
         const uint32_t smem_base = tc::smem_u32(smem);
         const uint32_t id = tc::idesc_bf16_f32(MM, CT_N, false);
@@ -1054,19 +985,9 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                     const bool first = kb == kb0;
 #pragma unroll
                     for (int j = 0; j < NS; ++j) {
-                        if (!tc::mbar_wait(&afull[r], pr, abort_flag, a.err)) {
-                            ok = false;
-                            break;
-                        }
-                        tc::tc_fence_after();
-                        issue_slice_gj<NS, NA, MAXL>(j, d, tmem + (uint32_t)(ACOL0 + 16 * r), dB, b_step, id, first);
-                        tc::mma_commit(&aempty[r]);
-                        if (++r == ASLOTS) {
-                            r = 0;
-                            pr ^= 1u;
-                        }
+                        const uint64_t dA = tc::sdesc_kmajor(smem_base + (uint32_t)(s * STAGE + j * BF_SLICE));
+                        issue_slice_gjs<NS, NA, MAXL>(j, d, dA, dB, b_step, id, first);
                     }
-                    if (!ok) break;
                     tc::mma_commit(&empty[s]);
                     if (++s == a.stages) {
                         s = 0;
@@ -1077,10 +998,11 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             }
         }
     } else if (warp >= 2) {
-        // ---- epilogue (warps 2-5 and 10-13, 32 columns each): per group, scale the six
-        // accumulators and add them into a double-float running sum; one FP64 tile per item
+        // ---- epilogue (warps 2-9, TMEM lane quarter warp % 4, 32 columns each): per group,
+        // scale the accumulators and add them into a double-float running sum; one FP64 tile
+        // per item
         const int q = warp % 4;
-        const int half = warp >= 10 ? 1 : 0;
+        const int half = warp >= 6 ? 1 : 0;
         const int r = q * 32 + (threadIdx.x % 32);
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
         constexpr int HC = CT_N / 2;
@@ -1442,6 +1364,13 @@ int oz_error_flag(OzState* o, cudaStream_t s) {
 
 namespace {
 
+using CtKernel = void (*)(const oz::CtArgs);
+// The contraction's instantiations: K = X X^T (partial tiles), the general product (8 digits,
+// direct), the non-symmetric K (direct).
+CtKernel ct_sym_kernel() { return oz::oz_contract_kernel<oz::NSL, oz::CT_NACC, oz::NSL - 1, false>; }
+CtKernel ct_gemm_kernel() { return oz::oz_contract_kernel<oz::GM_NS, oz::GM_NACC, oz::GM_MAXL, true>; }
+CtKernel ct_nonsym_kernel() { return oz::oz_contract_kernel<oz::NSL, oz::CT_NACC, oz::NSL - 1, true>; }
+
 // error word, SM count and kernel attributes, once per state
 int oz_prepare(OzState* o, cudaStream_t s, std::string& err) {
     using namespace oz;
@@ -1458,12 +1387,9 @@ int oz_prepare(OzState* o, cudaStream_t s, std::string& err) {
     }
     if (!o->attrs_set) {
         cudaFuncSetAttribute(oz_transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
-        cudaFuncSetAttribute(oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
-        cudaFuncSetAttribute(oz_contract_kernel<GM_NS, GM_NACC, GM_MAXL, GM_ASLOTS, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
-        cudaFuncSetAttribute(oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(ct_sym_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(ct_gemm_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
+        cudaFuncSetAttribute(ct_nonsym_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BUDGET);
         o->attrs_set = true;
     }
     return GDFJK_OK;
@@ -1721,8 +1647,7 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
             ca.stages = ct_stages;
             ca.n_items = o->ntiles_all;
             ca.err = o->err;
-            oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, true>
-                <<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+            ct_nonsym_kernel()<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
             continue;
         }
         // split over groups so that there are about two work items per SM
@@ -1752,8 +1677,7 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         ca.stages = ct_stages;
         ca.n_items = o->ntiles * nsplit;
         ca.err = o->err;
-        oz_contract_kernel<NSL, CT_NACC, NSL - 1, CT_ASLOTS, false>
-            <<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+        ct_sym_kernel()<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
         const size_t nl = (size_t)nbf * (nbf + 1) / 2;
         const int blocks = (int)std::min<size_t>((nl + 255) / 256, (size_t)o->num_sms * 16);
         oz_reduce_kernel<<<blocks, 256, 0, s>>>(o->part, nsplit, o->ntiles, nbf, o->d_tob, o->ncb, K, batch > 0 ? 1 : 0);
@@ -1887,8 +1811,7 @@ int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb
         ca.stages = ct_stages;
         ca.n_items = ca.ntiles;
         ca.err = o->err;
-        oz_contract_kernel<GM_NS, GM_NACC, GM_MAXL, GM_ASLOTS, true>
-            <<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
+        ct_gemm_kernel()<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
     }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the buffers are released on return
