@@ -345,7 +345,10 @@ class GpuDFJK:
         naux = self.df.naux if self.df is not None else self.aux.nbf
         flags = {"mixed": abi.MIXED, "fp64-emulated": abi.EMULATED}.get(self.precision, 0)
         flags |= abi.B_HOST if self.b_host else 0
-        return DFJKEngine.query_memory(nbf, naux, nbf, flags) // 8
+        total = DFJKEngine.query_memory(nbf, naux, nbf, flags)
+        if self.do_wK:  # two more tensors (J^-1 (Q|mn), (Q|w|mn)), each in its own engine
+            total += 2 * (total - DFJKEngine.query_memory(nbf, naux, nbf, flags | abi.B_HOST))
+        return total // 8
 
     def initialize(self):
         """preiterations(): build B on the host, upload it to HBM once."""

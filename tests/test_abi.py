@@ -53,3 +53,16 @@ def test_query_memory_leaves_host_b_out_without_gpu(jk_built):
     full = DFJKEngine.query_memory(1856, 4448, 160)
     host = DFJKEngine.query_memory(1856, 4448, 160, _jkabi.B_HOST)
     assert full - host == 4448 * 435 * 4096 * 8
+
+
+def test_memory_estimate_counts_wk_tensors_without_gpu(jk_built):
+    """GpuDFJK.memory_estimate (doubles, like JK::memory_estimate) adds the two wK tensors."""
+    from types import SimpleNamespace
+
+    from psi4_gb300.jk import GpuDFJK
+
+    jk = GpuDFJK(df_tensor=SimpleNamespace(nbf=384, naux=1856))
+    base = jk.memory_estimate()
+    jk.set_do_wK(True)
+    b_tiles = 1856 * (6 * 7 // 2) * 4096  # doubles of one tensor in tiles
+    assert jk.memory_estimate() - base == 2 * b_tiles
