@@ -21,12 +21,13 @@ def row_exponent(x):
     return np.where(m > 0, e, -100000)
 
 
-def digits(x, E):
-    """Balanced 7-bit digits (most significant first) of rows of x with |x| < 2^E."""
-    v = np.rint(np.ldexp(x, (7 * P - 2 - E)[..., None])).astype(np.int64)
-    u = v + OFF
-    assert (u >= 0).all() and (u < (1 << (7 * P))).all()
-    return np.stack([((u >> (7 * (P - 1 - s))) & 127) - 64 for s in range(P)], axis=0).astype(np.float64)
+def digits(x, E, p=P):
+    """Balanced 7-bit digits (most significant first, p of them) of rows of x with |x| < 2^E."""
+    off = 64 * sum(1 << (7 * s) for s in range(p))
+    v = np.rint(np.ldexp(x, (7 * p - 2 - E)[..., None])).astype(np.int64)
+    u = v + off
+    assert (u >= 0).all() and (u < (1 << (7 * p))).all()
+    return np.stack([((u >> (7 * (p - 1 - s))) & 127) - 64 for s in range(p)], axis=0).astype(np.float64)
 
 
 def _f32_rz(x):
@@ -36,23 +37,23 @@ def _f32_rz(x):
     return np.where(over, np.nextafter(r, np.float32(0)), r)
 
 
-def emulated_product(A, B, exact=EXACT, kstep=16):
+def emulated_product(A, B, exact=EXACT, kstep=16, p=P, max_level=MAX_LEVEL):
     """A (m x k) @ B (n x k)^T as the kernels form it: per-row exponents of both operands,
-    exact levels 0..exact, the remaining levels <= MAX_LEVEL in a round-toward-zero FP32 tail
-    updated once per pair and 16-deep k step."""
+    p digits, exact levels 0..exact, the remaining levels <= max_level in a round-toward-zero
+    FP32 tail updated once per pair and 16-deep k step."""
     EA, EB = row_exponent(A), row_exponent(B)
-    dA, dB = digits(A, EA), digits(B, EB)
+    dA, dB = digits(A, EA, p), digits(B, EB, p)
     total = np.zeros((A.shape[0], B.shape[0]))
-    for s in range(P):
-        for t in range(P):
+    for s in range(p):
+        for t in range(p):
             if s + t <= exact:
                 total += (dA[s] @ dB[t].T) * 2.0 ** (-7 * (s + t))  # exact integers
     tail = np.zeros_like(total, dtype=np.float32)
-    pairs = [(s, t) for s in range(P) for t in range(P) if exact < s + t <= MAX_LEVEL]
+    pairs = [(s, t) for s in range(p) for t in range(p) if exact < s + t <= max_level]
     for k0 in range(0, A.shape[1], kstep):
         for s, t in pairs:
-            p = (dA[s][:, k0:k0 + kstep] @ dB[t][:, k0:k0 + kstep].T) * 2.0 ** (-7 * (s + t))
-            tail = _f32_rz(tail.astype(np.float64) + p)
+            term = (dA[s][:, k0:k0 + kstep] @ dB[t][:, k0:k0 + kstep].T) * 2.0 ** (-7 * (s + t))
+            tail = _f32_rz(tail.astype(np.float64) + term)
     return np.ldexp(total + tail, EA[:, None] + EB[None, :] - 10)
 
 
@@ -97,3 +98,23 @@ def test_exact_level_bounds():
     for L in range(4):
         assert (L + 1) * 1024 * 64 * 64 <= 2**24
     assert 5 * 819 * 64 * 64 <= 2**24
+
+
+def test_metric_contraction_needs_eight_digits(ints_built):
+    """The metric contraction B = J^-1/2 (P|mn) on real integrals (water cc-pVTZ): J^-1/2 has
+    entries ~50 that cancel to |B| <= 1.06, and the digit error scales with row and column
+    maxima, not with each term.  The K build's scheme (7 digits, levels <= 6, levels 0-4 exact)
+    leaves ~7e-11 in B; the product kernel's (8 digits, levels <= 8, levels 0-5 exact) ~4e-14."""
+    from tests.helpers import system
+
+    mol, pb, ab, ints, df = system("h2o_scf2", "cc-pvtz")
+    A = ints.three_index(shell_mask=df.sparsity.shell_mask)
+    r, c = np.tril_indices(df.nbf)
+    A[:, ~df.sparsity.pair_mask[r, c]] = 0.0
+    assert df.naux <= 1024  # one accumulation run
+    e7 = np.abs(emulated_product(df.Jmhalf, A.T.copy(), exact=4, p=7, max_level=6) - df.B_tri).max()
+    e8 = np.abs(emulated_product(df.Jmhalf, A.T.copy(), exact=5, p=8, max_level=8) - df.B_tri).max()
+    print(f"water cc-pVTZ metric contraction: 7 digits {e7:.2e}, 8 digits {e8:.2e}")
+    assert e7 > 1e-11
+    assert e8 < 1e-12
+
