@@ -478,3 +478,7 @@ class GpuDFJK:
         if self.engine is not None:
             self.engine.close()
             self.engine = None
+        if self.wk_engines is not None:
+            for e in self.wk_engines:
+                e.close()
+            self.wk_engines = None
