@@ -36,7 +36,6 @@ namespace gdfjk {
 constexpr int MM = 128;                    // tile rows (MMA M)
 constexpr int MK = tc::SWZ / 2;            // k per pipeline stage: one swizzle row of bf16
 constexpr int A_TILE_BYTES = MM * MK * 2;  // 8 KB
-constexpr int U_ROW_ALIGN = 32;            // U^T column groups are padded to 32 rows
 constexpr int CN = 256;                    // contraction tile columns (MMA N)
 constexpr int SMEM_BUDGET = 224 * 1024;
 constexpr int SMEM_RESERVE = 2048;         // alignment slack + barriers
