@@ -184,12 +184,29 @@ void* gdfjk_stream(gdfjk_t h);
  *   J  device, nbf x nbf output, overwritten with J_mn = sum_Q B_Q,mn sum_ls B_Q,ls D_ls
  * The fitted density d_Q is kept in a fixed file-scope device array of
  * GDFJK_NOALLOC_MAX_NAUX doubles (512 KB) that every GPU loading the library holds until
- * exit; naux above that limit is rejected with GDFJK_ERR_ARG.  The first call on a device
- * resolves the array's device address (cudaGetSymbolAddress): make that first call before
- * any stream capture.  All calls share the array and each overwrites it completely before
- * reading it; calls whose work overlaps on the GPU race on it.  Errors: gdfjk_last_error(NULL). */
+ * exit; naux above that limit is rejected with GDFJK_ERR_ARG.  Every call looks up the
+ * array's device address in the calling thread's current CUDA context (cudaGetSymbolAddress,
+ * which allocates nothing); the first call in a context may load the module, so make that
+ * first call before any stream capture.  All calls share the array and each overwrites it
+ * completely before reading it; calls whose work overlaps on the GPU race on it.
+ * Errors: gdfjk_last_error(NULL). */
 #define GDFJK_NOALLOC_MAX_NAUX 65536
 int gdfjk_coulomb_noalloc(int nbf, int naux, const double* B, const double* D, double* J, void* stream);
+
+/* Host-side fault injection for the failure tests (no counterpart in the reference, whose
+ * failures are PSIEXCEPTIONs from the allocator and the integral code):
+ *   gdfjk_debug_refuse_allocations(after, count)  of the device (and pinned host)
+ *       allocations the engine makes from now on, the first `after` go through and the next
+ *       `count` are refused as out of memory, exactly as a full device refuses them, so the
+ *       GDFJK_ERR_OOM paths (release the other form's copy of B and retry once) run;
+ *       count = 0 ends the injection.  Process-wide.  Returns the number of refusals of
+ *       the previous setting that were still pending (>= 0), or GDFJK_ERR_ARG.
+ *   gdfjk_debug_wait_probe(h, limit_s)  runs the tensor-core kernels' bounded mbarrier wait on
+ *       a barrier that nothing arrives on, with the limit limit_s (0 < limit_s <= 10) instead
+ *       of the production 2 s: the kernel gives up, raises its wait error bit and returns, and
+ *       the call returns GDFJK_ERR_DEVICE; the handle stays usable. */
+int gdfjk_debug_refuse_allocations(int after, int count);
+int gdfjk_debug_wait_probe(gdfjk_t h, double limit_s);
 
 int gdfjk_destroy(gdfjk_t h);
 const char* gdfjk_last_error(gdfjk_t h);

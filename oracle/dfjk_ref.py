@@ -33,9 +33,25 @@ def compute_D(C_left, C_right=None):
     return C_left @ C_right.T
 
 
-def compute_J_symm(Ppq, sp, D, nbf, naux):
+class RowTables:
+    """Per-row significant-column lists of a sparsity, built once (outside any timed region),
+    as psi4 builds schwarz_fun_index_ and the symm_* tables once in prepare_sparsity
+    (dfhelper.cc:368-420) and its loops then index with them:
+      full[k]   significant n of row k, ascending (the columns of B[k] in pQq order)
+      sym[k]    the m >= k part (columns symm_ignored_columns[k] .. +symm_small_skips[k])
+      wsym[k]   compute_J_symm's density weights on sym[k]: 1 on the diagonal, 2 off it
+                (dfhelper.cc:3186-3192)."""
+
+    def __init__(self, sp, nbf):
+        self.full = [np.flatnonzero(sp.fun_index[k]) for k in range(nbf)]
+        self.sym = [ms[ms >= k] for k, ms in enumerate(self.full)]
+        self.wsym = [np.where(ms == k, 1.0, 2.0) for k, ms in enumerate(self.sym)]
+
+
+def compute_J_symm(Ppq, sp, D, nbf, naux, tables=None):
     """dfhelper.cc:3162-3223 for one density, the whole aux range as one block (bcount=0,
-    block_size=naux, AO_core).  Returns J (nbf x nbf)."""
+    block_size=naux, AO_core).  Returns J (nbf x nbf).  `tables` (RowTables) replaces the
+    per-row index construction by the precomputed lists; the arithmetic is the same."""
     T1 = np.zeros(naux)
     # pass 1: (Qm)(m) -> (Q), rows k, m >= k significant, off-diagonal weight 2
     for k in range(nbf):
@@ -45,8 +61,11 @@ def compute_J_symm(Ppq, sp, D, nbf, naux):
         jump = int(sp.big_skips[k])
         if mi == 0:
             continue
-        ms = [m for m in range(k, nbf) if sp.fun_index[k, m]]
-        Dbuf = np.array([D[k, m] if m == k else 2.0 * D[k, m] for m in ms])
+        if tables is None:
+            ms = [m for m in range(k, nbf) if sp.fun_index[k, m]]
+            Dbuf = np.array([D[k, m] if m == k else 2.0 * D[k, m] for m in ms])
+        else:
+            Dbuf = D[k, tables.sym[k]] * tables.wsym[k]
         blk = Ppq[jump: jump + naux * si].reshape(naux, si)[:, skip: skip + mi]
         T1 += blk @ Dbuf
     # pass 2: J_km = sum_Q B[k][Q][m] d_Q over the m >= k part, then unpack + symmetrise
@@ -60,13 +79,19 @@ def compute_J_symm(Ppq, sp, D, nbf, naux):
             continue
         blk = Ppq[jump: jump + naux * si].reshape(naux, si)[:, skip: skip + mi]
         T2 = T1 @ blk
-        ms = [m for m in range(k, nbf) if sp.fun_index[k, m]]
-        for c, m in enumerate(ms):
-            if m == k:
-                J[k, k] += T2[c]
-            else:
-                J[k, m] += T2[c]
-                J[m, k] += T2[c]
+        if tables is None:
+            ms = [m for m in range(k, nbf) if sp.fun_index[k, m]]
+            for c, m in enumerate(ms):
+                if m == k:
+                    J[k, k] += T2[c]
+                else:
+                    J[k, m] += T2[c]
+                    J[m, k] += T2[c]
+        else:
+            ms = tables.sym[k]
+            J[k, ms] += T2
+            off = ms != k
+            J[ms[off], k] += T2[off]
     return J
 
 
@@ -91,28 +116,29 @@ def compute_J(Ppq, sp, D, nbf, naux):
     return J
 
 
-def first_transform_pQq(Ppq, sp, Cmat, nbf, naux):
-    """dfhelper.cc:2162-2186: T[k][Q][i] = sum_{m in sig(k)} B[k][Q][m] C[m][i]."""
+def first_transform_pQq(Ppq, sp, Cmat, nbf, naux, tables=None):
+    """dfhelper.cc:2162-2186: T[k][Q][i] = sum_{m in sig(k)} B[k][Q][m] C[m][i] (the rows of C
+    gathered per k, then one DGEMM per row)."""
     nocc = Cmat.shape[1]
     T = np.zeros((nbf, naux, nocc))
     for k in range(nbf):
         si = int(sp.small_skips[k])
         if si == 0:
             continue
-        ms = [m for m in range(nbf) if sp.fun_index[k, m]]
+        ms = [m for m in range(nbf) if sp.fun_index[k, m]] if tables is None else tables.full[k]
         blk = Ppq[int(sp.big_skips[k]): int(sp.big_skips[k]) + naux * si].reshape(naux, si)
         T[k] = blk @ Cmat[ms, :]
     return T
 
 
-def compute_K(Ppq, sp, C_left, C_right, nbf, naux, lr_symmetric=True):
+def compute_K(Ppq, sp, C_left, C_right, nbf, naux, lr_symmetric=True, tables=None):
     """dfhelper.cc:3350-3377: K += T1 T2^T with inner dimension nocc*naux; nocc=0 skips."""
     nocc = C_left.shape[1]
     K = np.zeros((nbf, nbf))
     if nocc == 0:
         return K
-    T1 = first_transform_pQq(Ppq, sp, C_left, nbf, naux).reshape(nbf, naux * nocc)
-    T2 = T1 if lr_symmetric else first_transform_pQq(Ppq, sp, C_right, nbf, naux).reshape(nbf, naux * nocc)
+    T1 = first_transform_pQq(Ppq, sp, C_left, nbf, naux, tables).reshape(nbf, naux * nocc)
+    T2 = T1 if lr_symmetric else first_transform_pQq(Ppq, sp, C_right, nbf, naux, tables).reshape(nbf, naux * nocc)
     K += T1 @ T2.T
     return K
 

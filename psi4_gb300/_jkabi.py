@@ -25,6 +25,8 @@ SIGNATURES = {
     "gdfjk_synchronize": (I, [P, D]),
     "gdfjk_stream": (P, [P]),
     "gdfjk_coulomb_noalloc": (I, [I, I, P, P, P, P]),
+    "gdfjk_debug_refuse_allocations": (I, [I, I]),
+    "gdfjk_debug_wait_probe": (I, [P, D]),
     "gdfjk_destroy": (I, [P]),
     "gdfjk_last_error": (ctypes.c_char_p, [P]),
 }

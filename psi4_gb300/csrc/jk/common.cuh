@@ -46,6 +46,12 @@ cudaError_t big_alloc(void** p, size_t bytes, bool host);
 void big_free(void* p);
 bool is_host_memory(const void* p);
 
+// Every device or pinned allocation of the engine goes through engine_malloc, which
+// cudaMalloc's unless a host-side fault injection (gdfjk_debug_refuse_allocations) asks it
+// to refuse: it then returns cudaErrorMemoryAllocation without allocating.
+cudaError_t engine_malloc(void** p, size_t bytes);
+bool alloc_refused();
+
 }  // namespace gdfjk
 
 // kernels (defined in j_kernels.cu / k_fp64.cu); all enqueue on `stream`.

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -35,9 +36,33 @@ int gdfjk::report_error(int code, const std::string& msg) {
     return code;
 }
 
+namespace {
+// fault injection: let g_alloc_pass allocations through, then refuse g_alloc_refuse
+std::mutex g_alloc_mutex;
+long g_alloc_pass = 0, g_alloc_refuse = 0;
+}  // namespace
+
+bool gdfjk::alloc_refused() {
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    if (g_alloc_refuse <= 0) return false;
+    if (g_alloc_pass > 0) {
+        --g_alloc_pass;
+        return false;
+    }
+    --g_alloc_refuse;
+    return true;
+}
+
+cudaError_t gdfjk::engine_malloc(void** p, size_t bytes) {
+    *p = nullptr;
+    if (alloc_refused()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
 cudaError_t gdfjk::big_alloc(void** p, size_t bytes, bool host) {
     *p = nullptr;
-    if (!host) return cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (!host) return engine_malloc(p, std::max<size_t>(bytes, 16));
+    if (alloc_refused()) return cudaErrorMemoryAllocation;
     void* hp = nullptr;
     cudaError_t e = cudaHostAlloc(&hp, std::max<size_t>(bytes, 16), cudaHostAllocMapped | cudaHostAllocPortable);
     if (e != cudaSuccess) return e;
@@ -127,7 +152,7 @@ int dalloc(gdfjk_t h, T** p, size_t n) {
         *p = nullptr;
     }
     if (n == 0) return GDFJK_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    cudaError_t e = engine_malloc(reinterpret_cast<void**>(p), n * sizeof(T));
     if (e != cudaSuccess) {
         cudaGetLastError();
         char buf[160];
@@ -162,7 +187,10 @@ int alloc_B(gdfjk_t h) {
 int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym, bool need_x) {
     int rc;
     size_t np2 = (size_t)h->nbf_pad * h->nbf_pad;
-    if (!h->D) {
+    // a group is (re)allocated whole unless every member exists, and a capacity is cleared
+    // before its buffers are replaced, so that a refused allocation never leaves a buffer
+    // missing behind a capacity that claims it
+    if (!h->D || !h->Dw || !h->dq || !h->Jt || !h->Kt) {
         if ((rc = dalloc(h, &h->D, np2))) return rc;
         if ((rc = dalloc(h, &h->Dw, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS))) return rc;
         if ((rc = dalloc(h, &h->dq, (size_t)std::max(h->naux, 1)))) return rc;
@@ -171,6 +199,7 @@ int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym, bool need_x) {
         if ((rc = dalloc(h, &h->Kt, (size_t)nout_full * TILE_ELEMS))) return rc;
     }
     if (nocc_pad > h->cap_nocc) {
+        h->cap_nocc = -1;
         if ((rc = dalloc(h, &h->Cl, (size_t)h->nbf_pad * std::max(nocc_pad, 1)))) return rc;
         if ((rc = dalloc(h, &h->Cr, (size_t)h->nbf_pad * std::max(nocc_pad, 1)))) return rc;
         h->cap_nocc = nocc_pad;
@@ -178,6 +207,7 @@ int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym, bool need_x) {
     if (!need_x) return GDFJK_OK;
     if (nocc_pad > h->cap_x || (nonsym && !h->Xr && nocc_pad > 0)) {
         int cap = std::max(nocc_pad, h->cap_x);
+        h->cap_x = 0;
         size_t xe = (size_t)h->nbf_pad * h->naux * cap;
         if ((rc = dalloc(h, &h->Xl, xe))) return rc;
         if (nonsym || h->Xr) {
@@ -191,6 +221,7 @@ int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym, bool need_x) {
     int nout = nonsym ? h->nT * h->nT : h->nT * (h->nT + 1) / 2;
     size_t need = (size_t)ns * nout * TILE_ELEMS;
     if (need > h->Kpart_elems) {
+        h->Kpart_elems = 0;
         if ((rc = dalloc(h, &h->Kpart, need))) return rc;
         h->Kpart_elems = need;
     }
@@ -474,7 +505,7 @@ int gdfjk_upload_B_block(gdfjk_t h, const double* Bq, int q0, int nq) {
     // staged through the host-path buffer in sub-blocks of at most 512 MB
     const int sub = (int)std::max<size_t>(1, std::min<size_t>((size_t)nq, (size_t)(512u << 20) / (npair * 8)));
     double* stage = nullptr;
-    if (cudaMalloc(&stage, (size_t)sub * npair * 8) != cudaSuccess) {
+    if (engine_malloc((void**)&stage, (size_t)sub * npair * 8) != cudaSuccess) {
         cudaGetLastError();
         return set_err(h, GDFJK_ERR_OOM, "upload_B_block: staging buffer refused");
     }
@@ -555,8 +586,8 @@ int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_sk
         }
     };
     for (int k = 0; k < 2; ++k) {
-        if (cudaMallocHost(&host_stage[k], (size_t)chunk * npair * 8) != cudaSuccess ||
-            cudaMalloc(&dev_stage[k], (size_t)chunk * npair * 8) != cudaSuccess ||
+        if (alloc_refused() || cudaMallocHost(&host_stage[k], (size_t)chunk * npair * 8) != cudaSuccess ||
+            engine_malloc((void**)&dev_stage[k], (size_t)chunk * npair * 8) != cudaSuccess ||
             cudaEventCreate(&done[k]) != cudaSuccess) {
             cudaGetLastError();
             cleanup();
@@ -632,12 +663,13 @@ int gdfjk_compute(gdfjk_t h, const double* C_left, const double* C_right, int no
     int rc;
     size_t n2 = (size_t)h->nbf * h->nbf;
     size_t cin = (size_t)h->nbf * std::max(ldc, 1);
-    if (!h->dJ) {
+    if (!h->dJ || !h->dK || !h->dD) {
         if ((rc = dalloc(h, &h->dJ, n2))) return rc;
         if ((rc = dalloc(h, &h->dK, n2))) return rc;
         if ((rc = dalloc(h, &h->dD, n2))) return rc;
     }
     if (cin > h->dCin_elems) {
+        h->dCin_elems = 0;
         if ((rc = dalloc(h, &h->dCin, cin))) return rc;
         if ((rc = dalloc(h, &h->dCrin, cin))) return rc;
         h->dCin_elems = cin;
@@ -671,12 +703,13 @@ int gdfjk_compute_wK(gdfjk_t hl, gdfjk_t hr, const double* C_left, const double*
     int rc;
     const size_t n2 = (size_t)h->nbf * h->nbf;
     const size_t cin = (size_t)h->nbf * std::max(ldc, 1);
-    if (!h->dJ) {
+    if (!h->dJ || !h->dK || !h->dD) {
         if ((rc = dalloc(h, &h->dJ, n2))) return rc;
         if ((rc = dalloc(h, &h->dK, n2))) return rc;
         if ((rc = dalloc(h, &h->dD, n2))) return rc;
     }
     if (cin > h->dCin_elems) {
+        h->dCin_elems = 0;
         if ((rc = dalloc(h, &h->dCin, cin))) return rc;
         if ((rc = dalloc(h, &h->dCrin, cin))) return rc;
         h->dCin_elems = cin;
@@ -737,12 +770,13 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
     CK(cudaSetDevice(h->device));
     int rc;
     size_t n2 = (size_t)h->nbf * h->nbf;
-    if (!h->dJ) {
+    if (!h->dJ || !h->dK || !h->dD) {
         if ((rc = dalloc(h, &h->dJ, n2)) || (rc = dalloc(h, &h->dK, n2)) || (rc = dalloc(h, &h->dD, n2))) return rc;
     }
     size_t cin = (size_t)h->nbf * std::max(ldc, 1), uin = (size_t)h->nbf * std::max(ldu, 1);
     size_t need = std::max(cin, uin);
     if (need > h->dCin_elems) {
+        h->dCin_elems = 0;
         if ((rc = dalloc(h, &h->dCin, need)) || (rc = dalloc(h, &h->dCrin, need))) return rc;
         h->dCin_elems = need;
     }
@@ -803,13 +837,14 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
     if (rc) return rc;
     size_t np2 = (size_t)nbf_pad * nbf_pad, n2 = (size_t)nbf * nbf;
     size_t npair = (size_t)nbf * (nbf + 1) / 2;
-    if (!h->gJp) {
+    if (!h->gJp || !h->gKp || !h->Jg || !h->gq || !h->Dw2 || !h->Jgt) {
         if ((rc = dalloc(h, &h->gJp, np2)) || (rc = dalloc(h, &h->gKp, np2)) || (rc = dalloc(h, &h->Jg, np2)) ||
             (rc = dalloc(h, &h->gq, (size_t)naux)) || (rc = dalloc(h, &h->Dw2, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS)) ||
             (rc = dalloc(h, &h->Jgt, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS)))
             return rc;
     }
     if (nocc_pad > h->bw_cap_nocc) {
+        h->bw_cap_nocc = -1;
         int nqb = back_transform_qblocks(naux);
         if ((rc = dalloc(h, &h->Yb, (size_t)nbf_pad * naux * nocc_pad)) ||
             (rc = dalloc(h, &h->Zpart, (size_t)nqb * nbf_pad * nocc_pad)) ||
@@ -878,6 +913,25 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
         return check_device_flag(h);
     }
     return GDFJK_OK;
+}
+
+int gdfjk_debug_refuse_allocations(int after, int count) {
+    if (after < 0 || count < 0) return set_err(nullptr, GDFJK_ERR_ARG, "debug_refuse_allocations: negative count");
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    const long pending = g_alloc_refuse;
+    g_alloc_pass = after;
+    g_alloc_refuse = count;
+    return (int)std::min<long>(pending, 1 << 30);
+}
+
+int gdfjk_debug_wait_probe(gdfjk_t h, double limit_s) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "wait_probe: null handle");
+    if (!(limit_s > 0.0) || limit_s > 10.0) return set_err(h, GDFJK_ERR_ARG, "wait_probe: limit must be in (0, 10] s");
+    CK(cudaSetDevice(h->device));
+    int rc = mixed_wait_probe(h->mixed, (unsigned long long)(limit_s * 1e9), h->stream, h->err);
+    if (rc) return set_err(h, rc, h->err);
+    if ((rc = wait_stream(h, env_timeout()))) return rc;
+    return check_device_flag(h);
 }
 
 int gdfjk_trim(gdfjk_t h) {

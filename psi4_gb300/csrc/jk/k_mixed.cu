@@ -501,7 +501,7 @@ size_t mixed_query_memory(int nbf, int naux, int max_nocc) {
 static int dalloc_bytes(void** p, size_t bytes, std::string& err) {
     big_free(*p);
     *p = nullptr;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = engine_malloc(p, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
         err = "mixed: device allocation of " + std::to_string(bytes / 1e9) + " GB refused";
@@ -542,6 +542,7 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
     }
     if (!m->B_ready || m->nbf_p != nbf_p) {
         size_t bytes = (size_t)naux * m->nnz * (MM * MK) * 2;
+        m->B_ready = false;
         if ((rc = dalloc_bytes((void**)&m->Bh, bytes, err)) || (rc = dalloc_bytes((void**)&m->Bl, bytes, err))) return rc;
         split_B_kernel<<<(unsigned)((size_t)naux * nbf_p), 256, 0, s>>>(B, naux, nbf, L.nT, L.ntiles, L.map, nbf_p,
                                                                        m->d_mb_ptr, m->d_mb_kb, m->nnz, m->Bh, m->Bl);
@@ -558,12 +559,14 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
     }
     size_t ue = (size_t)nu_pad * nbf_p;
     if (ue > m->U_cap) {
+        m->U_cap = 0;
         if ((rc = dalloc_bytes((void**)&m->Uh, ue * 2, err)) || (rc = dalloc_bytes((void**)&m->Ul, ue * 2, err))) return rc;
         m->U_cap = ue;
     }
     const unsigned long long kdim = (unsigned long long)naux * nu_pad;
     size_t xe = (size_t)nbf_p * kdim;
     if (xe > m->X_cap) {
+        m->X_cap = 0;
         if ((rc = dalloc_bytes((void**)&m->Xh, xe * 2, err)) || (rc = dalloc_bytes((void**)&m->Xl, xe * 2, err))) return rc;
         m->X_cap = xe;
     }
@@ -647,6 +650,7 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
     nsplit = (nkb_total + kb_per_split - 1) / kb_per_split;
     size_t pe = (size_t)nsplit * ntiles_out * MM * CN;
     if (pe > m->part_cap) {
+        m->part_cap = 0;
         if ((rc = dalloc_bytes((void**)&m->part, pe * 4, err))) return rc;
         m->part_cap = pe;
     }
@@ -675,6 +679,8 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
     // ---- fixed-order FP64 reduction (+ running K for incremental builds)
     size_t kn = (size_t)nbf * nbf;
     if (kn > m->Kacc_cap) {
+        m->Kacc_cap = 0;
+        m->have_prev = false;
         if ((rc = dalloc_bytes((void**)&m->Kacc, kn * 8, err))) return rc;
         m->Kacc_cap = kn;
         m->have_prev = false;
@@ -695,6 +701,38 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
     return GDFJK_OK;
 }
 
+namespace {
+// The bounded wait of the tensor-core kernels (tc::mbar_wait) on an mbarrier that no thread
+// and no copy ever arrives on: nothing is in flight, so the block simply returns once the
+// wait has run out and raised its error bit.
+__global__ void wait_probe_kernel(unsigned long long limit_ns, int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        abort_flag = 0;
+        tc::fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) tc::mbar_wait(&bar, 0, &abort_flag, err, limit_ns);
+}
+}  // namespace
+
+int mixed_wait_probe(MixedState* m, unsigned long long limit_ns, cudaStream_t s, std::string& err) {
+    int rc;
+    if (!m->err) {
+        if ((rc = dalloc_bytes((void**)&m->err, sizeof(int), err))) return rc;
+        cudaMemsetAsync(m->err, 0, sizeof(int), s);
+    }
+    wait_probe_kernel<<<1, 32, 0, s>>>(limit_ns, m->err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("wait probe: launch failed: ") + cudaGetErrorString(e);
+        return GDFJK_ERR_CUDA;
+    }
+    return GDFJK_OK;
+}
+
 int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, const int* map_host, int nbf, int nbf_pad,
                   int naux, const double* Cpad, int nocc, int nocc_pad, int mode, double* K, cudaEvent_t ev_transform_done,
                   cudaStream_t stream, std::string& err) {
@@ -707,6 +745,8 @@ int mixed_build_K(MixedState* m, const double* B, const TileLayout& L, const int
 int mixed_set_base(MixedState* m, const double* K, int nbf, cudaStream_t s, std::string& err) {
     size_t kn = (size_t)nbf * nbf;
     if (kn > m->Kacc_cap) {
+        m->Kacc_cap = 0;
+        m->have_prev = false;
         int rc = dalloc_bytes((void**)&m->Kacc, kn * 8, err);
         if (rc) return rc;
         m->Kacc_cap = kn;

@@ -87,6 +87,11 @@ __device__ __forceinline__ int exp_of_max_f(unsigned bits) {
     if (ex == 0) ex = 1;
     return ex - 126;
 }
+// Non-finite inputs (Inf / NaN bits in a maximum) would turn into finite digit garbage, so
+// the exponent kernels raise the numeric error bit instead (the host returns GDFJK_ERR_NUMERIC).
+constexpr unsigned long long NONFINITE_BITS = 0x7FF0000000000000ull;
+constexpr int DEV_ERR_NUMERIC = 4;
+
 // 2^(E-5) as a float (the slice weight of a row); 0 for empty rows or below the normal range
 __device__ __forceinline__ float scale_of(int E) {
     if (E == E_EMPTY) return 0.f;
@@ -176,7 +181,8 @@ __device__ __forceinline__ float slice_weight(int s) { return __int_as_float((12
 // Row maxima of |B_Q[m][.]| over both triangles from the stored tiles: rows of a stored tile
 // (I, J) belong to rows 64I+r, and for I != J its columns to rows 64J+c.
 __global__ void oz_rowmax_kernel(const double* __restrict__ B, int ntiles, const int* __restrict__ tI,
-                                 const int* __restrict__ tJ, int nbf_p, unsigned long long* __restrict__ rowmax) {
+                                 const int* __restrict__ tJ, int nbf_p, unsigned long long* __restrict__ rowmax,
+                                 int* __restrict__ err) {
     const size_t qt = blockIdx.x;  // Q * ntiles + t
     const int Q = (int)(qt / ntiles), t = (int)(qt % ntiles);
     const int I = tI[t], J = tJ[t];
@@ -193,6 +199,7 @@ __global__ void oz_rowmax_kernel(const double* __restrict__ B, int ntiles, const
         mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
         mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
         if (part == 0 && mx) atomicMax(&rowmax[(size_t)Q * nbf_p + I * TILE + r], mx);
+        if (part == 0 && mx >= NONFINITE_BITS) atomicOr(err, DEV_ERR_NUMERIC);
     }
     if (I != J) {
         int c = threadIdx.x % TILE, part = threadIdx.x / TILE;
@@ -206,6 +213,7 @@ __global__ void oz_rowmax_kernel(const double* __restrict__ B, int ntiles, const
         if (threadIdx.x < TILE) {
             unsigned long long m2 = max(max(colpart[0][c], colpart[1][c]), max(colpart[2][c], colpart[3][c]));
             if (m2) atomicMax(&rowmax[(size_t)Q * nbf_p + J * TILE + c], m2);
+            if (m2 >= NONFINITE_BITS) atomicOr(err, DEV_ERR_NUMERIC);
         }
     }
 }
@@ -277,7 +285,7 @@ __global__ void __launch_bounds__(256) oz_split_B_kernel(const double* __restric
 // ---------------------------------------------------------------- digits of C (every build)
 // Column exponents of C (nbf x nocc_pad, row-major): one block per column slot i < ncols.
 __global__ void oz_col_scale_kernel(const double* __restrict__ C, int nbf, int nocc_pad, int nocc,
-                                    int* __restrict__ eC, float* __restrict__ sC) {
+                                    int* __restrict__ eC, float* __restrict__ sC, int* __restrict__ err) {
     const int i = blockIdx.x;
     unsigned long long mx = 0;
     if (i < nocc)
@@ -296,6 +304,7 @@ __global__ void oz_col_scale_kernel(const double* __restrict__ C, int nbf, int n
         const int E = exp_of_max_d(m2);
         eC[i] = E;
         sC[i] = scale_of(E);
+        if (m2 >= NONFINITE_BITS) atomicOr(err, DEV_ERR_NUMERIC);
     }
 }
 
@@ -1117,7 +1126,7 @@ __global__ void oz_reduce_kernel(const double* __restrict__ part, int nsplit, in
 
 // Exponent and weight of A's row m in group g: one warp per (m, g).
 __global__ void oz_gemm_rowexp_kernel(const double* __restrict__ A, size_t lda, int M, int K, int kw, int ngroups,
-                                      int M_pad, int* __restrict__ Ea, float* __restrict__ Sa) {
+                                      int M_pad, int* __restrict__ Ea, float* __restrict__ Sa, int* __restrict__ err) {
     const int wid = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32), lane = threadIdx.x % 32;
     if (wid >= M_pad * ngroups) return;
     const int m = wid % M_pad, g = wid / M_pad;
@@ -1134,12 +1143,13 @@ __global__ void oz_gemm_rowexp_kernel(const double* __restrict__ A, size_t lda, 
         const int E = exp_of_max_d(mx);
         Ea[(size_t)g * M_pad + m] = E;
         Sa[(size_t)g * M_pad + m] = scale_of(E);
+        if (mx >= NONFINITE_BITS) atomicOr(err, DEV_ERR_NUMERIC);
     }
 }
 
 // Exponent and weight of B's column n in group g: one thread per (n, g), coalesced over n.
 __global__ void oz_gemm_colexp_kernel(const double* __restrict__ B, size_t ldb, int N, int K, int kw, int ngroups,
-                                      int N_pad, int* __restrict__ Eb, float* __restrict__ Sb) {
+                                      int N_pad, int* __restrict__ Eb, float* __restrict__ Sb, int* __restrict__ err) {
     const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (id >= (size_t)N_pad * ngroups) return;
     const int n = (int)(id % N_pad), g = (int)(id / N_pad);
@@ -1154,6 +1164,7 @@ __global__ void oz_gemm_colexp_kernel(const double* __restrict__ B, size_t ldb, 
     const int E = exp_of_max_d(mx);
     Eb[(size_t)g * N_pad + n] = E;
     Sb[(size_t)g * N_pad + n] = scale_of(E);
+    if (mx >= NONFINITE_BITS) atomicOr(err, DEV_ERR_NUMERIC);
 }
 
 // Eight consecutive values -> the GM_NS BF16 slices of their digits, packed in uint4s.
@@ -1288,7 +1299,7 @@ int oz_alloc(void** p, size_t bytes, std::string& err) {
         cudaFree(*p);
         *p = nullptr;
     }
-    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    cudaError_t e = engine_malloc(p, std::max<size_t>(bytes, 16));
     if (e != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
@@ -1429,12 +1440,14 @@ static int oz_ensure_digits(OzState* o, const double* B, const TileLayout& L, co
     // ---- digits of B (once per upload), the listed blocks only
     if (!o->B_ready || o->nbf_p != nbf_p) {
         const size_t rows = (size_t)naux * nbf_p;
+        o->B_ready = false;
         if ((rc = oz_alloc((void**)&o->rowmax, rows * 8, err)) || (rc = oz_alloc((void**)&o->sA, rows * 4, err)) ||
             (rc = oz_alloc((void**)&o->Bd, (size_t)naux * o->nnz * I8_BLOCK, err)))
             return rc;
         cudaMemsetAsync(o->rowmax, 0, rows * 8, s);
         if (L.ntiles > 0)
-            oz_rowmax_kernel<<<(unsigned)((size_t)naux * L.ntiles), 256, 0, s>>>(B, L.ntiles, L.tI, L.tJ, nbf_p, o->rowmax);
+            oz_rowmax_kernel<<<(unsigned)((size_t)naux * L.ntiles), 256, 0, s>>>(B, L.ntiles, L.tI, L.tJ, nbf_p, o->rowmax,
+                                                                                   o->err);
         oz_split_B_kernel<<<(unsigned)((size_t)naux * o->nnz), 256, 0, s>>>(
             B, nbf, L.nT, L.ntiles, L.map, nbf_p, o->nnz, o->d_blk_mb, o->d_mb_kb, o->d_mb_ptr, o->rowmax, o->sA, o->Bd);
         o->nbf_p = nbf_p;
@@ -1467,24 +1480,28 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     const int N = round_up((nocc_p + nchunk - 1) / nchunk, 16);
     const int ncols = nchunk * N;
     if ((size_t)ncols > o->sc_cap) {
+        o->sc_cap = 0;
         if ((rc = oz_alloc((void**)&o->eC, ncols * sizeof(int), err)) || (rc = oz_alloc((void**)&o->sC, ncols * 4, err)))
             return rc;
         o->sc_cap = ncols;
     }
     const size_t ce = (size_t)ncols * nbf_p * NSL;
     if (ce > o->C_cap) {
+        o->C_cap = 0;
         if ((rc = oz_alloc((void**)&o->Cd, ce * 2, err))) return rc;
         o->C_cap = ce;
     }
     const bool nonsym = Crpad != nullptr;
     if (nonsym) {
         if ((size_t)ncols > o->scr_cap) {
+            o->scr_cap = 0;
             if ((rc = oz_alloc((void**)&o->eC_r, ncols * sizeof(int), err)) ||
                 (rc = oz_alloc((void**)&o->sC_r, ncols * 4, err)))
                 return rc;
             o->scr_cap = ncols;
         }
         if (ce > o->Cr_cap) {
+            o->Cr_cap = 0;
             if ((rc = oz_alloc((void**)&o->Cd_r, ce * 2, err))) return rc;
             o->Cr_cap = ce;
         }
@@ -1494,7 +1511,7 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         int* eCs = side ? o->eC_r : o->eC;
         float* sCs = side ? o->sC_r : o->sC;
         __nv_bfloat16* Cds = side ? o->Cd_r : o->Cd;
-        oz_col_scale_kernel<<<ncols, 256, 0, s>>>(Cs, nbf, nocc_pad, nocc, eCs, sCs);
+        oz_col_scale_kernel<<<ncols, 256, 0, s>>>(Cs, nbf, nocc_pad, nocc, eCs, sCs, o->err);
         const size_t total = (size_t)ncols * (nbf_p / 8);
         const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)o->num_sms * 8);
         oz_split_C_kernel<<<blocks, 256, 0, s>>>(Cs, nbf, nbf_p, nocc_pad, N, ncols, eCs, Cds);
@@ -1505,6 +1522,7 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     int qb = (int)std::min<double>((double)naux, std::max<double>(G, std::floor(x_cap_bytes() / per_q / G) * G));
     qb = std::max(1, qb);
     if ((size_t)qb > o->X_cap) {
+        o->X_cap = 0;
         if ((rc = oz_alloc((void**)&o->Xdf, (size_t)nbf * qb * nocc_p * 8, err)) ||
             (rc = oz_alloc((void**)&o->Xd, (size_t)nbf_p * qb * nocc_p * NSL * 2, err)))
             return rc;
@@ -1512,19 +1530,23 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     }
     const int ngroups_max = (qb + G - 1) / G;
     if ((size_t)nbf * ngroups_max > o->xm_cap) {
+        o->xm_cap = 0;
         if ((rc = oz_alloc((void**)&o->xmax, (size_t)nbf * ngroups_max * 4, err))) return rc;
         o->xm_cap = (size_t)nbf * ngroups_max;
     }
     if ((size_t)nbf_p * ngroups_max > o->sx_cap) {
+        o->sx_cap = 0;
         if ((rc = oz_alloc((void**)&o->Sx, (size_t)nbf_p * ngroups_max * 4, err))) return rc;
         o->sx_cap = (size_t)nbf_p * ngroups_max;
     }
     if (nonsym) {
         if ((size_t)qb > o->Xr_cap) {
+            o->Xr_cap = 0;
             if ((rc = oz_alloc((void**)&o->Xd_r, (size_t)nbf_p * qb * nocc_p * NSL * 2, err))) return rc;
             o->Xr_cap = qb;
         }
         if ((size_t)nbf_p * ngroups_max > o->sxr_cap) {
+            o->sxr_cap = 0;
             if ((rc = oz_alloc((void**)&o->Sx_r, (size_t)nbf_p * ngroups_max * 4, err))) return rc;
             o->sxr_cap = (size_t)nbf_p * ngroups_max;
         }
@@ -1656,6 +1678,7 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         nsplit = (ngroups + gps - 1) / gps;
         const size_t pe = (size_t)nsplit * o->ntiles * MM * CT_N;
         if (pe > o->part_cap) {
+            o->part_cap = 0;
             if ((rc = oz_alloc((void**)&o->part, pe * 8, err))) return rc;
             o->part_cap = pe;
         }
@@ -1765,7 +1788,7 @@ int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb
     {
         const size_t warps = (size_t)M_pad * ngroups;
         oz_gemm_rowexp_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(A, lda, M, K, RUN_K, ngroups, M_pad, Ea,
-                                                                                      Sa);
+                                                                                      Sa, o->err);
         const size_t units = (size_t)M_pad * nkbt * (MK / 8);
         const int blocks = (int)std::min<size_t>((units + 255) / 256, (size_t)o->num_sms * 16);
         oz_gemm_split_A_kernel<<<blocks, 256, 0, s>>>(A, lda, M, K, M_pad, nkbt, kpg, Ea, Xd);
@@ -1783,7 +1806,7 @@ int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb
         }
         const size_t cols = (size_t)N_pad * ngroups;
         oz_gemm_colexp_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, s>>>(B + c0, ldb, ncc, K, RUN_K, ngroups, N_pad, Eb,
-                                                                              Sb);
+                                                                              Sb, o->err);
         const size_t units = (size_t)N_pad * nkbt * (MK / 8);
         const int blocks = (int)std::min<size_t>((units + 255) / 256, (size_t)o->num_sms * 16);
         oz_gemm_split_Bt_kernel<<<blocks, 256, 0, s>>>(B + c0, ldb, ncc, K, N_pad, nkbt, kpg, Eb, Yd);

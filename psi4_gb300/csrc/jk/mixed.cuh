@@ -31,5 +31,8 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
 int mixed_set_base(MixedState* m, const double* K, int nbf, cudaStream_t s, std::string& err);
 // error bits raised by the tensor-core kernels since the last call (0 = none); clears them
 int mixed_error_flag(MixedState* m, cudaStream_t s);
+// Failure test of the bounded waits: one thread waits on an mbarrier that nothing arrives on,
+// gives up after limit_ns and raises the wait error bit (2) in this state's flag word.
+int mixed_wait_probe(MixedState* m, unsigned long long limit_ns, cudaStream_t s, std::string& err);
 
 }  // namespace gdfjk

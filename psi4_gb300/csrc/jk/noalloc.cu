@@ -14,7 +14,6 @@
 // Both passes use fixed-order reductions, so results are reproducible.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -37,12 +36,22 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_pass1_kernel(const double*
     int Q = blockIdx.x;
     size_t npair = (size_t)nbf * (nbf + 1) / 2;
     const double* row = B + (size_t)Q * npair;
+    // One flat, coalesced walk over the packed triangle: thread t reads pairs t, t+256, ...
+    // and keeps its own (m, n) decoding of the packed index, advanced without a square root.
+    size_t p = threadIdx.x;
+    size_t m = 0, n = p;
+    while (m < (size_t)nbf && n > m) {
+        n -= m + 1;
+        ++m;
+    }
     double acc = 0.0;
-    for (int m = 0; m < nbf; ++m) {
-        const double* r = row + (size_t)m * (m + 1) / 2;
-        for (int n = threadIdx.x; n <= m; n += NA_THREADS) {
-            double w = (n == m) ? D[(size_t)m * nbf + m] : D[(size_t)m * nbf + n] + D[(size_t)n * nbf + m];
-            acc = fma(__ldg(r + n), w, acc);
+    for (; p < npair; p += NA_THREADS) {
+        double w = (n == m) ? D[m * nbf + m] : D[m * nbf + n] + D[n * nbf + m];
+        acc = fma(__ldg(row + p), w, acc);
+        n += NA_THREADS;
+        while (m < (size_t)nbf && n > m) {
+            n -= m + 1;
+            ++m;
         }
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -71,10 +80,6 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_pass2_kernel(const double*
     }
 }
 
-// Device address of the scratch array, resolved once per device.
-std::mutex g_addr_mutex;
-double* g_addr[64] = {nullptr};
-
 }  // namespace
 }  // namespace gdfjk
 
@@ -84,24 +89,15 @@ extern "C" int gdfjk_coulomb_noalloc(int nbf, int naux, const double* B, const d
     if (naux > GDFJK_NOALLOC_MAX_NAUX)
         return report_error(GDFJK_ERR_ARG, "coulomb_noalloc: naux " + std::to_string(naux) + " exceeds the fixed scratch of " +
                                                std::to_string(GDFJK_NOALLOC_MAX_NAUX) + " fitting functions");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return report_error(GDFJK_ERR_CUDA, std::string("coulomb_noalloc: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= 64) return report_error(GDFJK_ERR_ARG, "coulomb_noalloc: device index out of range");
-    double* dq = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_addr_mutex);
-        if (!g_addr[dev]) {
-            // set-up, once per device, with that device current: host code must use the
-            // device address, not the host-side name of the array
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_dq);
-            if (e != cudaSuccess)
-                return report_error(GDFJK_ERR_CUDA, std::string("coulomb_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_addr[dev] = static_cast<double*>(p);
-        }
-        dq = g_addr[dev];
-    }
+    // The array's device address belongs to the CUDA context current on this thread, so it
+    // is looked up on every call (no allocation; the first call in a context may load the
+    // module, which is why that first call should come before any stream capture).  A cached
+    // address would go stale after cudaDeviceReset or under a caller's own non-primary context.
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_dq);
+    if (e != cudaSuccess)
+        return report_error(GDFJK_ERR_CUDA, std::string("coulomb_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    double* dq = static_cast<double*>(p);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     noalloc_pass1_kernel<<<naux, NA_THREADS, 0, s>>>(B, D, nbf, dq);
     size_t npair = (size_t)nbf * (nbf + 1) / 2;

@@ -67,14 +67,16 @@ __device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t pa
     return ok != 0;
 }
 
-// Bounded wait on phase `parity` of `bar`; gives up when the block aborted or on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err) {
+// Bounded wait on phase `parity` of `bar`; gives up when the block aborted or after
+// `limit_ns` (WAIT_NS in every production kernel; the failure tests pass a short one).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err,
+                                          unsigned long long limit_ns = WAIT_NS) {
     if (mbar_try_wait(bar, parity)) return true;
     uint64_t t0 = global_timer();
     while (true) {
         if (mbar_try_wait_suspend(bar, parity, 100000u)) return true;
         if (*abort_flag) return false;
-        if (global_timer() - t0 > WAIT_NS) {
+        if (global_timer() - t0 > limit_ns) {
             *abort_flag = 1;
             atomicOr(err, 2);
             return false;

@@ -88,4 +88,6 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/psi4/share/psi4/basis")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_basis.py <psi4 source tree>/psi4/share/psi4/basis")
+    main(sys.argv[1])

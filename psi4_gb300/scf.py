@@ -43,6 +43,7 @@ class SCFResult:
     nocc: int
     timings: dict = field(default_factory=dict)
     log: list = field(default_factory=list)
+    orbitals: list = field(default_factory=list)
 
 
 def orthogonalizer(S, tol=1e-7):
@@ -56,24 +57,33 @@ def orthogonalizer(S, tol=1e-7):
 
 
 class DIIS:
+    """Pulay DIIS over at most `max_vec` (F, error) pairs; the error inner products are kept
+    between iterations, so adding a vector costs one product per stored vector."""
+
     def __init__(self, max_vec=10):
         self.max_vec = max_vec
         self.F, self.E = [], []
+        self.G = np.zeros((0, 0))
 
     def add(self, F, err):
-        self.F.append(F.copy())
-        self.E.append(err.copy())
-        if len(self.F) > self.max_vec:
+        if len(self.F) == self.max_vec:
             self.F.pop(0)
             self.E.pop(0)
+            self.G = self.G[1:, 1:]
+        self.F.append(F.copy())
+        self.E.append(err.copy())
+        n = len(self.E)
+        G = np.zeros((n, n))
+        G[:n - 1, :n - 1] = self.G
+        for i in range(n):
+            G[i, n - 1] = G[n - 1, i] = float(np.vdot(self.E[i], self.E[n - 1]))
+        self.G = G
 
     def extrapolate(self):
         n = len(self.F)
         B = -np.ones((n + 1, n + 1))
         B[n, n] = 0.0
-        for i in range(n):
-            for j in range(i + 1):
-                B[i, j] = B[j, i] = float(np.vdot(self.E[i], self.E[j]))
+        B[:n, :n] = self.G
         rhs = np.zeros(n + 1)
         rhs[n] = -1.0
         # scale for conditioning
@@ -140,9 +150,12 @@ class PrecisionSchedule:
 
 
 def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=None, diis_start=1,
-        fail_on_maxiter=True, callback=None, verbose=False, schedule: PrecisionSchedule | None = None) -> SCFResult:
+        fail_on_maxiter=True, callback=None, verbose=False, schedule: PrecisionSchedule | None = None,
+        record_orbitals=False) -> SCFResult:
     """Run RHF with a JK object exposing C_clear/C_left_add/compute/J/K.  With a
-    PrecisionSchedule the JK switches between the mixed and FP64 forms per iteration."""
+    PrecisionSchedule the JK switches between the mixed and FP64 forms per iteration.
+    `record_orbitals` keeps every iteration's occupied orbitals in ``result.orbitals`` (for
+    evaluating afterwards the FP64 energy at each iterate: `energy_errors_vs_fp64`)."""
     X = orthogonalizer(S)
     t0 = time.perf_counter()
     if guess_C is None:
@@ -160,8 +173,11 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
     converged = False
     it = 0
     F = J = K = D = None
+    orbitals = []
     for it in range(1, maxiter + 1):
         Cocc = np.ascontiguousarray(C[:, :nocc])
+        if record_orbitals:
+            orbitals.append(Cocc)
         D = Cocc @ Cocc.T
         jk.C_clear()
         jk.C_left_add(Cocc)
@@ -177,7 +193,8 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
         F = H + 2.0 * J - K
         E = e_nuc + 2.0 * np.vdot(D, H) + 2.0 * np.vdot(D, J) - np.vdot(D, K)
         energies.append(float(E))
-        grad = X.T @ (F @ D @ S - S @ D @ F) @ X
+        FDS = F @ (D @ S)
+        grad = X.T @ (FDS - FDS.T) @ X  # FDS - SDF: F, D and S are symmetric
         dnorm = float(np.sqrt(np.mean(grad * grad)))
         dE = E - E_old
         entry = {"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm}
@@ -210,10 +227,33 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
         eps, Cp = np.linalg.eigh(X.T @ Fd @ X)
         C = X @ Cp
     res = SCFResult(energies[-1], energies, it, converged, C, eps, D, F, J, K, nocc,
-                    {"total_s": time.perf_counter() - t0, "jk_s": t_jk}, log)
+                    {"total_s": time.perf_counter() - t0, "jk_s": t_jk}, log, orbitals)
     if not converged and fail_on_maxiter:
         raise SCFConvergenceError(f"Could not converge SCF iterations in {maxiter} iterations.", res)
     return res
+
+
+def rhf_energy(jk, Cocc, H, e_nuc):
+    """E = E_nuc + 2 tr(D H) + 2 tr(D J) - tr(D K) at the occupied orbitals Cocc, with J and
+    K from one build of `jk` in whatever form it is set to (RHF::compute_E, rhf.cc:308-370)."""
+    jk.C_clear()
+    jk.C_left_add(np.ascontiguousarray(Cocc))
+    jk.compute()
+    J, K = np.asarray(jk.J()[0]), np.asarray(jk.K()[0])
+    D = Cocc @ Cocc.T
+    return float(e_nuc + 2.0 * np.vdot(D, H) + 2.0 * np.vdot(D, J) - np.vdot(D, K))
+
+
+def energy_errors_vs_fp64(res: SCFResult, fp64_jk, H, e_nuc):
+    """For an SCF run with recorded orbitals: each iteration's energy minus the FP64 energy
+    at the same orbitals (one FP64 build of `fp64_jk` per iteration), written into
+    ``res.log[i]["energy_error_vs_fp64"]``; returns the list of errors."""
+    errs = []
+    for entry, Cocc in zip(res.log, res.orbitals):
+        e = entry["energy"] - rhf_energy(fp64_jk, Cocc, H, e_nuc)
+        entry["energy_error_vs_fp64"] = e
+        errs.append(e)
+    return errs
 
 
 def core_hamiltonian(ints):
@@ -273,8 +313,9 @@ def uhf(jk, H, S, nalpha, nbeta, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, 
         E = (e_nuc + np.vdot(Da + Db, H) + 0.5 * np.vdot(Da + Db, J) - 0.5 * np.vdot(Da, Ka)
              - 0.5 * np.vdot(Db, Kb))
         energies.append(float(E))
-        ga = X.T @ (Fa @ Da @ S - S @ Da @ Fa) @ X
-        gb = X.T @ (Fb @ Db @ S - S @ Db @ Fb) @ X
+        FDSa, FDSb = Fa @ (Da @ S), Fb @ (Db @ S)
+        ga = X.T @ (FDSa - FDSa.T) @ X
+        gb = X.T @ (FDSb - FDSb.T) @ X
         dnorm = float(np.sqrt(0.5 * (np.mean(ga * ga) + np.mean(gb * gb))))
         dE = E - E_old
         log.append({"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm})

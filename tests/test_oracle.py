@@ -106,3 +106,19 @@ def test_oracle_wk_against_dense(ints_built):
     sym = np.einsum("qmn,ni,qlk,ki->ml", M1, Cl, W, Cl)
     got = dfjk_ref.compute_wK(m1.to_pQq(), w.to_pQq(), df.sparsity, Cl, None, nbf, naux)
     assert np.abs(got - 0.5 * (sym + sym.T)).max() < 1e-12 * max(1.0, np.abs(sym).max())
+
+
+def test_row_tables_give_the_same_results(ints_built):
+    """The precomputed per-row index lists (RowTables, used by the timed CPU baseline) give
+    bitwise the loop restatement's J and K, on a screened layout."""
+    mol, pb, ab, ints, df = system("h2o_2_far", cutoff=1e-5)
+    sp = df.sparsity
+    nbf, naux = df.nbf, df.naux
+    Ppq = df.to_pQq()
+    tb = dfjk_ref.RowTables(sp, nbf)
+    C = random_orbitals(nbf, 7, 11)
+    D = dfjk_ref.compute_D(C)
+    assert np.array_equal(dfjk_ref.compute_J_symm(Ppq, sp, D, nbf, naux),
+                          dfjk_ref.compute_J_symm(Ppq, sp, D, nbf, naux, tb))
+    assert np.array_equal(dfjk_ref.compute_K(Ppq, sp, C, C, nbf, naux, True),
+                          dfjk_ref.compute_K(Ppq, sp, C, C, nbf, naux, True, tb))
