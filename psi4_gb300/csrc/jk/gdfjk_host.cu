@@ -283,7 +283,7 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
                             h->err);
             if (rc == GDFJK_ERR_OOM) {  // give the mixed form's split copy of B back and retry once
                 CK(cudaStreamSynchronize(s));
-                mixed_invalidate(h->mixed);
+                mixed_release(h->mixed);
                 rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, Cr, nocc, nocc_pad, K, h->ev[3], s,
                                 h->err);
             }
@@ -800,8 +800,17 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
         CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
     } else if (mode & GDFJK_DO_K) {
         CK(cudaEventRecord(h->ev[2], s));
-        rc = mixed_k_factor(h->mixed, h->B, layout_of(h), h->map.data(), h->nbf, h->naux, h->dCrin, std::max(ldu, 1), npos, nu - npos,
-                            (mode & GDFJK_RESET) ? 0 : 1, h->dK, h->ev[3], s, h->err);
+        auto factor = [&]() {
+            return mixed_k_factor(h->mixed, h->B, layout_of(h), h->map.data(), h->nbf, h->naux, h->dCrin,
+                                  std::max(ldu, 1), npos, nu - npos, (mode & GDFJK_RESET) ? 0 : 1, h->dK, h->ev[3], s,
+                                  h->err);
+        };
+        rc = factor();
+        if (rc == GDFJK_ERR_OOM) {  // give the emulated form's caches back and retry once
+            CK(cudaStreamSynchronize(s));
+            oz_release(h->oz);
+            rc = factor();
+        }
         if (rc) return rc;
         CK(cudaEventRecord(h->ev[4], s));
         launch_finite_check(h->dK, n2, h->d_err, s);
@@ -939,7 +948,7 @@ int gdfjk_trim(gdfjk_t h) {
     CK(cudaSetDevice(h->device));
     int rc = wait_stream(h, env_timeout());
     if (rc) return rc;
-    mixed_invalidate(h->mixed);
+    mixed_release(h->mixed);
     oz_release(h->oz);
     return GDFJK_OK;
 }

@@ -480,12 +480,17 @@ void mixed_destroy(MixedState* m) {
     delete m;
 }
 
-void mixed_invalidate(MixedState* m) {
+void mixed_release(MixedState* m) {
     if (!m) return;
     big_free(m->Bh);
     big_free(m->Bl);
     m->Bh = m->Bl = nullptr;
     m->B_ready = false;
+}
+
+void mixed_invalidate(MixedState* m) {
+    if (!m) return;
+    mixed_release(m);
     m->have_prev = false;
 }
 

@@ -14,6 +14,9 @@ MixedState* mixed_create();
 void mixed_destroy(MixedState* m);
 // B changed: drop the split copies and the incremental history.
 void mixed_invalidate(MixedState* m);
+// Memory pressure: drop the split copies of B (rebuilt on next use) but keep the incremental
+// history, which is still valid for the same B.
+void mixed_release(MixedState* m);
 size_t mixed_query_memory(int nbf, int naux, int max_nocc);
 // K for the lr-symmetric density C C^T (C padded, device), written to K (nbf x nbf, device).
 // map_host: the tile map of L on the host (the split copy of B keeps only the 128 x 32 blocks

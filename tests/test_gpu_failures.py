@@ -161,7 +161,7 @@ def test_refusal_at_every_allocation_of_a_build(ints_built, jk_built, form, coun
             break  # the build made no more than `after` allocations: every point was covered
     else:
         pytest.fail("the sweep did not reach the end of the build's allocations")
-    assert outcomes[-1] == "ok" and len(outcomes) > 3
+    assert outcomes[-1] == "ok" and len(outcomes) >= 2  # at least one refusal point inside the build
     if count == 2 or form == "native":
         assert "oom" in outcomes  # no retry absorbs these
 
@@ -178,3 +178,24 @@ def test_bounded_wait_runs_out_and_the_kernel_returns(ints_built, jk_built):
     J1, K1, _ = eng.compute(C, mode=FORMS["emulated"])
     assert np.array_equal(J0, J1) and np.array_equal(K0, K1)
     eng.close()
+
+
+def test_released_split_copy_keeps_the_incremental_history(ints_built, jk_built):
+    """Memory pressure (gdfjk_trim, or the other form's OOM retry) drops the precision form's
+    split copy of B but not the K it increments: the next increment after a release gives
+    bitwise the increment without one."""
+    from psi4_gb300.jk import density_difference_factor
+
+    mol, pb, ab, ints, df = system("h2o_2", "cc-pvdz", 1e-12)
+    C1 = _orbitals(df.nbf, 10, 5)
+    C2 = _orbitals(df.nbf, 10, 6)
+    U, npos = density_difference_factor(C2, C1)
+    out = []
+    for release in (False, True):
+        eng = _engine(df)
+        eng.compute_incremental(C1, C1, C1.shape[1], reset=True)
+        if release:
+            eng.trim()
+        out.append(eng.compute_incremental(C2, U, npos, reset=False))
+        eng.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
