@@ -20,6 +20,19 @@ TOL = 1e-10
 EMU = abi.DO_J | abi.DO_K | abi.EMULATED
 
 
+def _random_bound(Kref):
+    """Bound for random, unnormalised orbitals: 1e-10 + 1e-11 max|K|.
+
+    Why relative there: U(0,1) orbitals drive |X| and |K| to 1e3-1e5 (no physical density
+    does that), and the digits are fixed point relative to each row's (or row group's)
+    largest magnitude, so the emulation's error scales with max|K| (49-bit digits less the
+    double-float accumulation: ~1e-11 relative at worst) rather than with each element, as
+    FP64 rounding would.  On physical orbitals the absolute bar holds unchanged: see
+    test_emulated_scf_orbitals_strict here and tests/test_gpu_realsize.py (7e-12 at
+    (H2O)_32 cc-pVTZ and (H2O)_64 cc-pVDZ on real integrals)."""
+    return TOL + 1e-11 * np.abs(Kref).max()
+
+
 def _k_fp64(df, C):
     return dfjk_ref.compute_K(df.to_pQq(), df.sparsity, C, C, df.nbf, df.naux)
 
@@ -64,7 +77,7 @@ def test_emulated_random_orbitals(ints_built, jk_built, case, nocc):
     Kr = _k_fp64(df, C)
     err = np.abs(K - Kr).max()
     print(f"{case[0]}/{case[1]} nocc {nocc}: max|K| {np.abs(Kr).max():.3e} max|dK| {err:.2e}")
-    assert err < TOL + 1e-11 * np.abs(Kr).max()
+    assert err < _random_bound(Kr)
 
 
 def test_emulated_determinism_and_batches(ints_built, jk_built, monkeypatch):
@@ -108,7 +121,7 @@ def test_emulated_long_k_runs(jk_built):
     _, K, _ = eng.compute(C.cpu().numpy(), mode=abi.DO_K | abi.EMULATED)
     err = np.abs(K - Kr).max()
     print(f"nbf {nbf}: max|K| {np.abs(Kr).max():.3e} max|dK| {err:.2e}")
-    assert err < TOL + 1e-11 * np.abs(Kr).max()
+    assert err < _random_bound(Kr)
 
 
 def test_emulated_scf2_energy(ints_built, jk_built):
@@ -166,7 +179,7 @@ def test_emulated_block_sparse(jk_built):
     _, Ke, _ = eng.compute(C, mode=abi.DO_K | abi.EMULATED)
     err = np.abs(Ke - K64).max()
     print(f"block-sparse emulated K: max|K| {np.abs(K64).max():.3e} max|dK| {err:.2e}")
-    assert err < TOL + 1e-11 * np.abs(K64).max()
+    assert err < _random_bound(K64)
     eng.trim()
     _, Ke2, _ = eng.compute(C, mode=abi.DO_K | abi.EMULATED)
     assert np.array_equal(Ke, Ke2)
@@ -187,7 +200,7 @@ def test_emulated_nonsymmetric_pairs(ints_built, jk_built, case, nocc):
     err = np.abs(K - Kr).max()
     print(f"{case[0]} nocc {nocc}: max|K| {np.abs(Kr).max():.3e} max|dK| {err:.2e} (native {np.abs(K64 - Kr).max():.2e})")
     assert np.array_equal(J, J64)
-    assert err < TOL + 1e-11 * np.abs(Kr).max()
+    assert err < _random_bound(Kr)
     assert np.abs(K - K.T).max() > 0  # really non-symmetric
 
 

@@ -43,6 +43,16 @@ def _orbitals(seed, n=NOCC):
     return np.random.default_rng(seed).standard_normal((NBF, n)) * 0.1
 
 
+def _synthetic_bound(Kref):
+    """1e-10 + 1e-11 max|K| for the synthetic B (N(0, 0.02) on every pair, no decay with
+    distance) and unnormalised random orbitals used here: max|K| reaches 5e3, far beyond
+    any physical K, and the emulated digits are fixed point relative to each row's largest
+    magnitude, so the error scales with max|K| (2.9e-10 absolute at 5.3e3 here, 5e-14
+    relative).  On physical orbitals and real integrals at this same size the absolute bar
+    of 1e-10 holds (tests/test_gpu_realsize.py: 6.6e-12)."""
+    return 1e-10 + 1e-11 * np.abs(Kref).max()
+
+
 def test_fullsize_emulated_matches_native(engine):
     C = _orbitals(1)
     J64, K64, _ = engine.compute(C, mode=abi.DO_J | abi.DO_K)
@@ -50,7 +60,7 @@ def test_fullsize_emulated_matches_native(engine):
     assert np.array_equal(J64, Je)  # J is native FP64 in both
     err = np.abs(Ke - K64).max()
     print(f"C2 size: max|K| {np.abs(K64).max():.3e} max|dK| emulated vs native {err:.2e}")
-    assert err < 1e-10 + 1e-11 * np.abs(K64).max()
+    assert err < _synthetic_bound(K64)
 
 
 def test_fullsize_symmetry_repeatability_and_linearity(engine):
@@ -65,7 +75,7 @@ def test_fullsize_symmetry_repeatability_and_linearity(engine):
     dk = np.abs(Ka + Kb - K1).max()
     print(f"C2 size: J linearity {dj:.2e} (max|J| {np.abs(J1).max():.3e}), K additivity {dk:.2e}")
     assert dj < 1e-12 * np.abs(J1).max()
-    assert dk < 3 * (1e-10 + 1e-11 * np.abs(K1).max())  # three builds' errors
+    assert dk < 3 * _synthetic_bound(K1)  # three builds' errors
 
 
 def test_fullsize_host_b_j(engine):
