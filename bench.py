@@ -345,6 +345,7 @@ def run_gpu(args):
                     "peak_source": "bf16_tflops_sustained of measured (MEASURED_PEAKS.json): the kernel runs inside "
                                    "back-to-back builds",
                     "issued_bf16_flops_per_launch": issued, "algorithmic_fp64_flops_per_launch": flops_transform,
+                    "frac_unpadded": OZ_PAIRS * 2.0 * naux * nbf * nbf * nocc / kt / 1e12 / bf16_sus,
                     "fp64_equivalent_tflops": flops_transform / kt / 1e12,
                     "fp64_equivalent_frac_of_dgemm": flops_transform / kt / 1e12 / fp64_peak,
                     "note": f"{OZ_PAIRS} BF16 slice-pair products per FP64 multiply-add, padded sizes"}

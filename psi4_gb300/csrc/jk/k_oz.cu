@@ -30,7 +30,9 @@
 //   split            X -> BF16 digit slices with one exponent per (row, group of Q), a group
 //                    being <= 1024 contraction terms.
 //   contraction      K[m][n] = sum_groups 2^(E_m+E_n-10) sum_pairs ... : 128 x 64 tiles of the
-//                    lower triangle; A slices copied into tensor memory by four copier warps;
+//                    lower triangle; both operands from shared memory; the pairs of the exact
+//                    levels of one A slice issued as one wide MMA over the level regions, which
+//                    lie side by side in TMEM (19 MMAs per 16 k instead of 28);
 //                    one accumulation run per group, drained into a double-float running sum
 //                    in registers; split over groups; FP64 partials summed in a fixed order.
 // In both GEMMs one pipeline stage holds every digit slice of one 32-deep k block, and the
@@ -478,19 +480,32 @@ __device__ __forceinline__ void issue_slice_j(int j, const uint32_t* d, uint32_t
 }
 
 // The contraction's MMAs with NS digits and levels up to MAXL: A slice J (shared-memory
-// descriptor dA; 16 k = 2 descriptor units) against B slices t <= min(NS - 1, MAXL - J),
-// accumulator min(J + t, NA - 1)
+// descriptor dA; 16 k = 2 descriptor units) against B slices t <= min(NS - 1, MAXL - J).  The
+// exact level regions d[0..NA-2] lie side by side in TMEM (CT_N columns each) and the B slices
+// one after another in the stage (slice t at row t*CT_N), so the pairs of levels J..NA-2 are
+// one operand of NW*CT_N rows, issued as MMAs of up to 256 columns; the tail pairs (level
+// >= NA-1) follow one by one into d[NA-1].
 template <int NS, int NA, int MAXL, int J>
 __device__ __forceinline__ void issue_slice_gs(const uint32_t* d, uint64_t dA, uint64_t dB, uint64_t b_step, uint32_t id,
                                                bool first) {
     constexpr int TMAX = (NS - 1) < (MAXL - J) ? (NS - 1) : (MAXL - J);
+    constexpr int NW0 = NA - 1 - J < 0 ? 0 : NA - 1 - J;
+    constexpr int NW = NW0 < TMAX + 1 ? NW0 : TMAX + 1;  // B slices of the wide operand
+    constexpr int ROWS = NW * CT_N;
+    const uint32_t id0 = id & ~(0x3Fu << 17);
 #pragma unroll
     for (int ks = 0; ks < MK / 16; ++ks) {
+        const uint32_t fw = (first && ks == 0 && J == 0) ? 0u : 1u;
 #pragma unroll
-        for (int t = 0; t <= TMAX; ++t) {
-            const int L = J + t < NA - 1 ? J + t : NA - 1;
-            const uint32_t f = (first && ks == 0 && J == 0 && t <= NA - 1) ? 0u : 1u;
-            tc::mma_bf16(d[L], dA + (uint64_t)(2 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
+        for (int r0 = 0; r0 < ROWS; r0 += 256) {
+            const int n = ROWS - r0 < 256 ? ROWS - r0 : 256;
+            tc::mma_bf16(d[J] + (uint32_t)r0, dA + (uint64_t)(2 * ks), dB + (uint64_t)(r0 * 4 + 2 * ks),
+                         id0 | ((uint32_t)(n >> 3) << 17), fw);
+        }
+#pragma unroll
+        for (int t = NW; t <= TMAX; ++t) {
+            const uint32_t f = (first && ks == 0 && J == 0 && t == NA - 1) ? 0u : 1u;
+            tc::mma_bf16(d[NA - 1], dA + (uint64_t)(2 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
         }
     }
 }
@@ -597,8 +612,11 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
             }
         }
     } else if (warp >= 6 && warp < 10) {
-        // ---- converters: row `row` of every slice, int8 field (d + 64) -> BF16 d * 2^(-7 slice),
-        // two K elements per 32-bit TMEM column, into the next A slots, two slices per step
+        // ---- converters: row `row` of every slice, int8 field f = d + 64 in [0, 127] -> BF16
+        // d * 2^(-7 slice), two K elements per 32-bit TMEM column, into the next A slots, two
+        // slices per step.  A byte permute puts f under the BF16 exponent of 128 (bits
+        // 0x4300 | f are the value 128 + f = 192 + d, exactly), and one BF16x2 FMA gives
+        // (192 + d) w - 192 w = d w exactly: two instructions per two elements.
         const int q = warp % 4;
         const int row = q * 32 + (threadIdx.x % 32);
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
@@ -639,17 +657,17 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                         const uint4 q1 = *reinterpret_cast<const uint4*>(st + j * I8_SLICE + row * MK + 16);
                         const uint32_t words[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
                         const float w = slice_weight(j);
-                        const float off = -8388672.0f * w;
+                        const __nv_bfloat162 wv = __float2bfloat162_rn(w);            // 2^(-7j), exact
+                        const __nv_bfloat162 cv = __float2bfloat162_rn(-192.0f * w);  // exact
                         uint32_t o[16];
 #pragma unroll
                         for (int wi = 0; wi < 8; ++wi) {
 #pragma unroll
                             for (int hh = 0; hh < 2; ++hh) {
-                                const uint32_t b0 = __byte_perm(words[wi], 0x4B000000u, 0x7440u | (uint32_t)(2 * hh));
-                                const uint32_t b1 = __byte_perm(words[wi], 0x4B000000u, 0x7440u | (uint32_t)(2 * hh + 1));
-                                const float g0 = fmaf(__uint_as_float(b0), w, off);
-                                const float g1 = fmaf(__uint_as_float(b1), w, off);
-                                o[2 * wi + hh] = __byte_perm(__float_as_uint(g0), __float_as_uint(g1), 0x7632u);
+                                // bytes (f_{2hh}, 0x43, f_{2hh+1}, 0x43): low half the even k
+                                const uint32_t x = __byte_perm(words[wi], 0x43434343u, hh ? 0x5342u : 0x5140u);
+                                const __nv_bfloat162 g = __hfma2(*reinterpret_cast<const __nv_bfloat162*>(&x), wv, cv);
+                                o[2 * wi + hh] = *reinterpret_cast<const uint32_t*>(&g);
                             }
                         }
                         tmem_st16(lane_base + (uint32_t)(TR_ACOL0 + 16 * slot[jj]), o);
