@@ -145,6 +145,12 @@ int gdfjk_compute_wK(gdfjk_t h_left, gdfjk_t h_right, const double* C_left, cons
 int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
                               int mode, double* J, double* K);
 
+/* Same with device buffers (C, U, J, K), asynchronous on the handle's stream: a caller can
+ * enqueue J from the new orbitals first (mode GDFJK_DO_J), form the factor U of dD on the host
+ * meanwhile, and then enqueue the K increment (mode GDFJK_DO_K | GDFJK_MIXED). */
+int gdfjk_compute_incremental_device(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos,
+                                     int ldu, int mode, double* J, double* K);
+
 /* Reverse-mode derivative of one lr-symmetric build (the differentiation form):
  * given upstream gradients gJ = dE/dJ and gK = dE/dK (nbf x nbf, device or host per
  * `on_device`), returns

@@ -758,8 +758,12 @@ int gdfjk_compute_wK(gdfjk_t hl, gdfjk_t hr, const double* C_left, const double*
     return GDFJK_OK;
 }
 
-int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
-                              int mode, double* J, double* K) {
+}  // extern "C"
+
+namespace {
+
+int check_incremental_args(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
+                           int mode, const double* J, const double* K) {
     if (!h) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: null handle");
     if (!h->B_ready) return set_err(h, GDFJK_ERR_STATE, "compute_incremental: B has not been uploaded");
     if (nocc < 0 || (nocc > 0 && (!C || ldc < nocc))) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: bad C / nocc / ldc");
@@ -767,8 +771,59 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
         return set_err(h, GDFJK_ERR_ARG, "compute_incremental: bad U / nu / npos / ldu");
     if ((mode & GDFJK_DO_J) && !J) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: J output is NULL");
     if ((mode & GDFJK_DO_K) && !K) return set_err(h, GDFJK_ERR_ARG, "compute_incremental: K output is NULL");
-    CK(cudaSetDevice(h->device));
+    return GDFJK_OK;
+}
+
+// The incremental build on the handle's stream, all pointers on the device: J (FP64) from C;
+// K either a full FP64 anchor from C (kept as the base) or the base plus the split-BF16
+// increment of the factor U.
+int enqueue_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
+                        int mode, double* J, double* K) {
     int rc;
+    const size_t n2 = (size_t)h->nbf * h->nbf;
+    cudaStream_t s = h->stream;
+    if (mode & GDFJK_DO_J) {
+        rc = enqueue_build(h, nocc > 0 ? C : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_J, nullptr, J, nullptr);
+        if (rc) return rc;
+        launch_finite_check(J, n2, h->d_err, s);
+    }
+    if ((mode & GDFJK_DO_K) && !(mode & GDFJK_MIXED)) {
+        // FP64 anchor: a full FP64 K from C that becomes the base of later increments
+        rc = enqueue_build(h, nocc > 0 ? C : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_K | (mode & GDFJK_EMULATED),
+                           nullptr, nullptr, K);
+        if (rc) return rc;
+        rc = mixed_set_base(h->mixed, K, h->nbf, s, h->err);
+        if (rc) return rc;
+        launch_finite_check(K, n2, h->d_err, s);
+    } else if (mode & GDFJK_DO_K) {
+        CK(cudaEventRecord(h->ev[2], s));
+        auto factor = [&]() {
+            return mixed_k_factor(h->mixed, h->B, layout_of(h), h->map.data(), h->nbf, h->naux, U, std::max(ldu, 1), npos,
+                                  nu - npos, (mode & GDFJK_RESET) ? 0 : 1, K, h->ev[3], s, h->err);
+        };
+        rc = factor();
+        if (rc == GDFJK_ERR_OOM) {  // give the emulated form's caches back and retry once
+            CK(cudaStreamSynchronize(s));
+            oz_release(h->oz);
+            rc = factor();
+        }
+        if (rc) return rc;
+        CK(cudaEventRecord(h->ev[4], s));
+        launch_finite_check(K, n2, h->d_err, s);
+    }
+    CK(cudaGetLastError());
+    return GDFJK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos, int ldu,
+                              int mode, double* J, double* K) {
+    int rc = check_incremental_args(h, C, nocc, ldc, U, nu, npos, ldu, mode, J, K);
+    if (rc) return rc;
+    CK(cudaSetDevice(h->device));
     size_t n2 = (size_t)h->nbf * h->nbf;
     if (!h->dJ || !h->dK || !h->dD) {
         if ((rc = dalloc(h, &h->dJ, n2)) || (rc = dalloc(h, &h->dK, n2)) || (rc = dalloc(h, &h->dD, n2))) return rc;
@@ -783,45 +838,19 @@ int gdfjk_compute_incremental(gdfjk_t h, const double* C, int nocc, int ldc, con
     cudaStream_t s = h->stream;
     if (nocc > 0) CK(cudaMemcpyAsync(h->dCin, C, cin * 8, cudaMemcpyHostToDevice, s));
     if (nu > 0) CK(cudaMemcpyAsync(h->dCrin, U, uin * 8, cudaMemcpyHostToDevice, s));
-    // J (and D) in FP64 from C
-    if (mode & GDFJK_DO_J) {
-        rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_J, nullptr, h->dJ,
-                           nullptr);
-        if (rc) return rc;
-    }
-    if ((mode & GDFJK_DO_K) && !(mode & GDFJK_MIXED)) {
-        // FP64 anchor: a full FP64 K from C that becomes the base of later increments
-        rc = enqueue_build(h, nocc > 0 ? h->dCin : nullptr, nullptr, nocc, std::max(ldc, 1),
-                           GDFJK_DO_K | (mode & GDFJK_EMULATED), nullptr, nullptr, h->dK);
-        if (rc) return rc;
-        rc = mixed_set_base(h->mixed, h->dK, h->nbf, s, h->err);
-        if (rc) return rc;
-        launch_finite_check(h->dK, n2, h->d_err, s);
-        CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
-    } else if (mode & GDFJK_DO_K) {
-        CK(cudaEventRecord(h->ev[2], s));
-        auto factor = [&]() {
-            return mixed_k_factor(h->mixed, h->B, layout_of(h), h->map.data(), h->nbf, h->naux, h->dCrin,
-                                  std::max(ldu, 1), npos, nu - npos, (mode & GDFJK_RESET) ? 0 : 1, h->dK, h->ev[3], s,
-                                  h->err);
-        };
-        rc = factor();
-        if (rc == GDFJK_ERR_OOM) {  // give the emulated form's caches back and retry once
-            CK(cudaStreamSynchronize(s));
-            oz_release(h->oz);
-            rc = factor();
-        }
-        if (rc) return rc;
-        CK(cudaEventRecord(h->ev[4], s));
-        launch_finite_check(h->dK, n2, h->d_err, s);
-        CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
-    }
-    if (mode & GDFJK_DO_J) {
-        launch_finite_check(h->dJ, n2, h->d_err, s);
-        CK(cudaMemcpyAsync(J, h->dJ, n2 * 8, cudaMemcpyDeviceToHost, s));
-    }
+    if ((rc = enqueue_incremental(h, h->dCin, nocc, ldc, h->dCrin, nu, npos, ldu, mode, h->dJ, h->dK))) return rc;
+    if (mode & GDFJK_DO_K) CK(cudaMemcpyAsync(K, h->dK, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if (mode & GDFJK_DO_J) CK(cudaMemcpyAsync(J, h->dJ, n2 * 8, cudaMemcpyDeviceToHost, s));
     if ((rc = wait_stream(h, env_timeout()))) return rc;
     return check_device_flag(h);
+}
+
+int gdfjk_compute_incremental_device(gdfjk_t h, const double* C, int nocc, int ldc, const double* U, int nu, int npos,
+                                     int ldu, int mode, double* J, double* K) {
+    int rc = check_incremental_args(h, C, nocc, ldc, U, nu, npos, ldu, mode, J, K);
+    if (rc) return rc;
+    CK(cudaSetDevice(h->device));
+    return enqueue_incremental(h, C, nocc, ldc, U, nu, npos, ldu, mode, J, K);
 }
 
 int gdfjk_synchronize(gdfjk_t h, double timeout_s) {

@@ -146,6 +146,12 @@ class DFJKEngine:
                                                      _p(U) if nu else None, nu, int(npos), max(nu, 1), m, _p(J), _p(K)))
         return J, K
 
+    def compute_incremental_device(self, C_ptr, nocc, ldc, U_ptr, nu, npos, ldu, mode, J_ptr, K_ptr):
+        """gdfjk_compute_incremental_device: device buffers, asynchronous on the engine's stream."""
+        vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
+        self._check(self.L.gdfjk_compute_incremental_device(self.h, vp(C_ptr), int(nocc), int(ldc), vp(U_ptr), int(nu),
+                                                            int(npos), int(ldu), int(mode), vp(J_ptr), vp(K_ptr)))
+
     def compute_device(self, Cl_ptr, Cr_ptr, nocc, ldc, mode, D_ptr, J_ptr, K_ptr):
         vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
         self._check(self.L.gdfjk_compute_device(self.h, vp(Cl_ptr), vp(Cr_ptr), int(nocc), int(ldc), int(mode), vp(D_ptr),
@@ -196,6 +202,20 @@ class DFJKEngine:
             self.close()
         except Exception:
             pass
+
+
+_POOL = None
+
+
+def _host_pool():
+    """One worker thread for host work that overlaps a GPU call (numpy's LAPACK and the
+    engine's ctypes calls both release the interpreter lock)."""
+    global _POOL
+    if _POOL is None:
+        from concurrent.futures import ThreadPoolExecutor
+
+        _POOL = ThreadPoolExecutor(max_workers=1, thread_name_prefix="gdfjk-host")
+    return _POOL
 
 
 def density_difference_factor(C_new, C_old, tol=1e-13):
@@ -425,8 +445,8 @@ class GpuDFJK:
             for i, Cl in enumerate(self._Cl):
                 Cr = None if lr_symmetric else self._Cr[i]
                 self._wK.append(left.compute_wK(right, Cl, Cr, mode=emu))
-        if self.precision in ("fp64", "fp64-emulated") and self.incremental and lr_symmetric and self.do_K and \
-                len(self._Cl) == 1:
+        single = lr_symmetric and len(self._Cl) == 1 and self._Cl[0].shape[1] > 0
+        if self.precision in ("fp64", "fp64-emulated") and self.incremental and single and self.do_K:
             # FP64 re-anchor of the precision form: full FP64 K, kept as the incremental base
             C = self._Cl[0]
             J, K = self.engine.compute_incremental(C, C, C.shape[1],
@@ -434,24 +454,37 @@ class GpuDFJK:
             self._C_prev = C.copy()
             self._J.append(J if self.do_J else None)
             self._K.append(K)
-            self._D.append(C @ C.T)
+            self._D = None
             self.last_timings = self.engine.timings()
             return
-        if self.precision == "mixed" and lr_symmetric and self.do_K and len(self._Cl) == 1:
-            # the precision form: K from the split-BF16 tensor-core path, incremental over dD
+        if self.precision == "mixed" and single and self.do_K:
+            # the precision form: K from the split-BF16 tensor-core path, incremental over dD.
+            # The FP64 J of the new orbitals runs on the GPU while the host factors dD (both
+            # calls release the interpreter lock), then the K increment.
             C = self._Cl[0]
-            jmode = (abi.DO_J if self.do_J else 0) | abi.DO_K | abi.MIXED
             if self.incremental and self._C_prev is not None and self._C_prev.shape == C.shape:
-                U, npos = density_difference_factor(C, self._C_prev)
-                J, K = self.engine.compute_incremental(C, U, npos, mode=jmode, reset=False)
+                fut = _host_pool().submit(density_difference_factor, C, self._C_prev)
+                J = self.engine.compute(C, mode=abi.DO_J)[0] if self.do_J else None
+                U, npos = fut.result()
+                _, K = self.engine.compute_incremental(C, U, npos, mode=abi.DO_K | abi.MIXED, reset=False)
                 self.last_rank = U.shape[1]
             else:
-                J, K = self.engine.compute_incremental(C, C, C.shape[1], mode=jmode, reset=True)
+                J, K = self.engine.compute_incremental(C, C, C.shape[1], mode=(abi.DO_J if self.do_J else 0) | abi.DO_K
+                                                       | abi.MIXED, reset=True)
+                J = J if self.do_J else None
                 self.last_rank = C.shape[1]
             self._C_prev = C.copy()
-            self._J.append(J if self.do_J else None)
+            self._J.append(J)
             self._K.append(K)
-            self._D.append(C @ C.T)
+            self._D = None
+            self.last_timings = self.engine.timings()
+            return
+        if single:
+            self._C_prev = None
+            J, K, _ = self.engine.compute(self._Cl[0], None, mode=mode)
+            self._J.append(J if self.do_J else None)
+            self._K.append(K if self.do_K else None)
+            self._D = None
             self.last_timings = self.engine.timings()
             return
         self._C_prev = None
@@ -472,6 +505,8 @@ class GpuDFJK:
         return self._K
 
     def D(self):
+        if self._D is None:  # formed on request (JK::compute_D, jk.cc:314-354)
+            self._D = [C @ C.T for C in self._Cl]
         return self._D
 
     def finalize(self):

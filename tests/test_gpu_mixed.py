@@ -118,3 +118,36 @@ def test_mixed_block_sparse(jk_built):
     err = np.abs(Km - K64).max() / np.abs(K64).max()
     print(f"block-sparse mixed K rel err {err:.2e}")
     assert err < REL_TOL
+
+
+def test_incremental_device_entry_matches_host_entry(ints_built, jk_built):
+    """gdfjk_compute_incremental_device (device buffers, asynchronous) gives bitwise the host
+    entry's J and K, for a full split build and an increment, and so does J enqueued on its
+    own before the K increment (the order GpuDFJK uses to overlap the host's factor of dD)."""
+    torch = pytest.importorskip("torch")
+    mol, pb, ab, ints, df = system("h2o_2", "cc-pvdz")
+    nbf = df.nbf
+    C1 = np.linalg.qr(np.random.default_rng(31).standard_normal((nbf, 10)))[0] * 0.5
+    C2 = C1 + 0.01 * np.random.default_rng(32).standard_normal((nbf, 10))
+    U, npos = density_difference_factor(C2, C1)
+    host = DFJKEngine(nbf, df.naux, None)
+    host.upload_qtri(df.B_tri)
+    host.compute_incremental(C1, C1, 10, reset=True)
+    Jh, Kh = host.compute_incremental(C2, U, npos)
+    dev = DFJKEngine(nbf, df.naux, None)
+    dev.upload_qtri(df.B_tri)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    C1d, C2d, Ud = t(C1), t(C2), t(U)
+    Jd = torch.empty((nbf, nbf), dtype=torch.float64, device="cuda")
+    Kd = torch.empty_like(Jd)
+    torch.cuda.synchronize()
+    m = abi.DO_J | abi.DO_K | abi.MIXED
+    dev.compute_incremental_device(C1d.data_ptr(), 10, 10, C1d.data_ptr(), 10, 10, 10, m | abi.RESET, Jd.data_ptr(),
+                                   Kd.data_ptr())
+    dev.compute_incremental_device(C2d.data_ptr(), 10, 10, None, 0, 0, 1, abi.DO_J, Jd.data_ptr(), None)
+    dev.compute_incremental_device(C2d.data_ptr(), 10, 10, Ud.data_ptr(), U.shape[1], npos, U.shape[1],
+                                   abi.DO_K | abi.MIXED, None, Kd.data_ptr())
+    dev.synchronize()
+    assert np.array_equal(Jd.cpu().numpy(), Jh) and np.array_equal(Kd.cpu().numpy(), Kh)
+    host.close()
+    dev.close()
