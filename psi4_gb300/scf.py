@@ -56,6 +56,14 @@ def orthogonalizer(S, tol=1e-7):
     return V[:, keep] / np.sqrt(w[keep])
 
 
+def _gradient(F, Cocc, S, X):
+    """X^T (F D S - S D F) X for D = Cocc Cocc^T without forming F D S: with A = X^T F Cocc and
+    B = X^T S Cocc it is A B^T - B A^T (F, S symmetric), O(nbf^2 nocc) instead of O(nbf^3)."""
+    A = X.T @ (F @ Cocc)
+    B = X.T @ (S @ Cocc)
+    return A @ B.T - B @ A.T
+
+
 class DIIS:
     """Pulay DIIS over at most `max_vec` (F, error) pairs; the error inner products are kept
     between iterations, so adding a vector costs one product per stored vector."""
@@ -193,8 +201,7 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
         F = H + 2.0 * J - K
         E = e_nuc + 2.0 * np.vdot(D, H) + 2.0 * np.vdot(D, J) - np.vdot(D, K)
         energies.append(float(E))
-        FDS = F @ (D @ S)
-        grad = X.T @ (FDS - FDS.T) @ X  # FDS - SDF: F, D and S are symmetric
+        grad = _gradient(F, Cocc, S, X)  # X^T (FDS - SDF) X
         dnorm = float(np.sqrt(np.mean(grad * grad)))
         dE = E - E_old
         entry = {"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm}
@@ -313,9 +320,8 @@ def uhf(jk, H, S, nalpha, nbeta, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, 
         E = (e_nuc + np.vdot(Da + Db, H) + 0.5 * np.vdot(Da + Db, J) - 0.5 * np.vdot(Da, Ka)
              - 0.5 * np.vdot(Db, Kb))
         energies.append(float(E))
-        FDSa, FDSb = Fa @ (Da @ S), Fb @ (Db @ S)
-        ga = X.T @ (FDSa - FDSa.T) @ X
-        gb = X.T @ (FDSb - FDSb.T) @ X
+        ga = _gradient(Fa, Ca_occ, S, X)
+        gb = _gradient(Fb, Cb_occ, S, X)
         dnorm = float(np.sqrt(0.5 * (np.mean(ga * ga) + np.mean(gb * gb))))
         dE = E - E_old
         log.append({"iter": it, "energy": float(E), "dE": float(dE), "dnorm": dnorm})
