@@ -443,6 +443,11 @@ def run_gpu(args):
             torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(nbf, naux, nocc)
+    if rank == 0 and args.grad_config:
+        try:
+            out["gradient"] = measure_gradient(args.grad_config, dev)
+        except Exception as ex:
+            out["gradient"] = {"unavailable": str(ex)[:300]}
     if rank == 0 and args.scf:
         try:
             out["scf"] = (measure_scf_device_B(args.scf_config, dev) if args.scf_config in ("c2", "c3")
@@ -933,6 +938,56 @@ def measure_scf(cfg):
             "time_to_converge_speedup": t64 / tmx}
 
 
+def measure_gradient(cfg, dev):
+    """The differentiation form at a configuration: SCF to convergence in the emulated FP64
+    form on real integrals, then the analytic nuclear gradient — the engine's backward (dE/dB
+    with (Q|mi) recomputed), the metric products G3 = M^-1/2 Gamma and W = Gamma A^T on the
+    tensor cores, and the derivative-integral contractions on the host — each piece timed."""
+    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.dfhelper import build_df_tensor
+    from psi4_gb300.grad import rhf_gradient
+    from psi4_gb300.ints import Integrals
+    from psi4_gb300.jk import GpuDFJK
+    from psi4_gb300.molecule import water_cluster
+    from psi4_gb300.scf import core_hamiltonian, rhf
+
+    gen, basis, desc = CONFIGS[cfg]
+    mol = water_cluster(*gen["lattice"], seed=0)
+    pb = BasisSet.build(mol, basis)
+    ab = BasisSet.fitting_for(mol, pb)
+    t0 = time.perf_counter()
+    ints = Integrals(mol, pb, ab)
+    df = build_df_tensor(mol, pb, ab, ints=ints)
+    H, S = core_hamiltonian(ints), ints.overlap()
+    t_init = time.perf_counter() - t0
+    nocc = mol.nelectron // 2
+    jk = GpuDFJK.from_tensor(df, device=dev.index or 0)
+    jk.initialize()
+    jk.set_precision("fp64-emulated")
+    ts = time.perf_counter()
+    res = rhf(jk, H, S, nocc, mol.nuclear_repulsion_energy(), e_conv=1e-10, d_conv=1e-10)
+    t_scf = time.perf_counter() - ts
+    C = res.C[:, :nocc]
+    D = C @ C.T
+    jk.engine.backward(C, 2.0 * D, -D, want_dC=False)  # warm: the backward's workspaces
+    tg = time.perf_counter()
+    _, Gamma = jk.engine.backward(C, 2.0 * D, -D, want_dC=False)
+    t_back = time.perf_counter() - tg
+    tm = {}
+    ta = time.perf_counter()
+    g = rhf_gradient(mol, ints, df, res, Gamma, engine=jk.engine, timings=tm)
+    t_assemble = time.perf_counter() - ta
+    tm_host = {}
+    gh = rhf_gradient(mol, ints, df, res, Gamma, timings=tm_host)  # the metric products on the host, for comparison
+    jk.finalize()
+    return {"workload": desc + " (real integrals, e_conv 1e-10, d_conv 1e-10)", "nbf": df.nbf, "naux": df.naux,
+            "nocc": nocc, "init_s": t_init, "scf_s": t_scf, "scf_iterations": res.iterations,
+            "gradient_s": t_back + t_assemble, "backward_gpu_s": t_back, "assembly_s": t_assemble,
+            "assembly_pieces_s": tm, "metric_products_host_fp64_s": tm_host.get("metric_products_s"),
+            "max_abs_gradient_difference_tensor_core_vs_host_products": float(np.abs(g - gh).max()),
+            "max_abs_gradient": float(np.abs(g).max())}
+
+
 def run_reference(args):
     """The reference arm: the CPU restatement of psi4's MemDFJK J + K (the oracle port; psi4
     itself cannot be built here) on the workload, rank 0 only.  Each step is one J + K build
@@ -988,6 +1043,7 @@ def main():
     ap.add_argument("--scf", type=int, default=1)
     ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
                     help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
+    ap.add_argument("--grad-config", default="c4", help="analytic-gradient leg ('' for none)")
     ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
     ap.add_argument("--metric", default="c2", help="configuration of the metric-contraction leg, '' for none")
     ap.add_argument("--host-b", default="c4,c2",

@@ -110,6 +110,15 @@ int gdfjk_upload_B_device_block(gdfjk_t h, const double* B_qtri_rows_device, int
 int gdfjk_metric_contract_device(gdfjk_t h, const double* metric, const double* Pmn, int ncols, int64_t ldp, double* B,
                                  int64_t ldb, int accumulate);
 
+/* The same digit product as a general matrix product, for the gradient's contractions with the
+ * metric (DFJKGrad's (A|B)^-1/2 applications and the 2-index density, jk_grad.cc:634-832):
+ *   C (+)= A op(B),  A M x K (lda), op(B) = B (K x N, ldb) for transb = 0 or B^T (B N x K,
+ *   ldb) for transb != 0, C M x N (ldc); all row-major device buffers, C must not overlap A
+ *   or B.  Runs on the handle's stream with temporary device buffers (the digits of A and of
+ *   one column chunk of op(B)) and returns when C is complete. */
+int gdfjk_gemm_device(gdfjk_t h, int transb, int M, int N, int K, const double* A, int64_t lda, const double* B,
+                      int64_t ldb, double* C, int64_t ldc, int accumulate);
+
 /* One Fock build, host buffers (JK::compute, jk.cc:595-681, for one density):
  *   C_left  nbf x nocc (row-major, leading dimension ldc >= nocc)
  *   C_right nbf x nocc or NULL (NULL = lr-symmetric: D = C_left C_left^T, jk.cc:597-599)

@@ -15,6 +15,7 @@ SIGNATURES = {
     "gdfjk_upload_B_device_block": (I, [P, P, I, I]),
     "gdfjk_trim": (I, [P]),
     "gdfjk_metric_contract_device": (I, [P, P, P, I, ctypes.c_int64, P, ctypes.c_int64, I]),
+    "gdfjk_gemm_device": (I, [P, I, I, I, I, P, ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64, I]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_wK": (I, [P, P, P, P, I, I, I, P]),

@@ -559,6 +559,19 @@ int gdfjk_metric_contract_device(gdfjk_t h, const double* metric, const double* 
     return check_device_flag(h);
 }
 
+int gdfjk_gemm_device(gdfjk_t h, int transb, int M, int N, int K, const double* A, int64_t lda, const double* B,
+                      int64_t ldb, double* C, int64_t ldc, int accumulate) {
+    if (!h || !A || !B || !C) return set_err(h, GDFJK_ERR_ARG, "gemm_device: null argument");
+    if (M < 0 || N < 0 || K < 1 || lda < K || ldb < (transb ? K : N) || ldc < N)
+        return set_err(h, GDFJK_ERR_ARG, "gemm_device: invalid sizes or leading dimensions");
+    CK(cudaSetDevice(h->device));
+    if (!h->oz) h->oz = oz_create();
+    int rc = oz_gemm(h->oz, A, (size_t)lda, B, (size_t)ldb, C, (size_t)ldc, M, N, K, accumulate, h->stream, h->err,
+                     transb ? 1 : 0);
+    if (rc) return set_err(h, rc, "gemm_device: " + h->err);
+    return check_device_flag(h);
+}
+
 int gdfjk_upload_B(gdfjk_t h, const double* B, int layout, const int64_t* big_skips, const int64_t* small_skips,
                    const int64_t* fun_index) {
     if (!h || !B) return set_err(h, GDFJK_ERR_ARG, "upload_B: null argument");

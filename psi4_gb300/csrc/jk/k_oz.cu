@@ -1765,10 +1765,11 @@ struct GemmBuffers {
 }  // namespace
 
 int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb, double* C, size_t ldc, int M, int N,
-            int K, int accumulate, cudaStream_t s, std::string& err) {
+            int K, int accumulate, cudaStream_t s, std::string& err, int transb) {
     using namespace oz;
     int rc;
-    if (M < 0 || N < 0 || K < 1 || !A || !B || !C || lda < (size_t)K || ldb < (size_t)N || ldc < (size_t)N) {
+    if (M < 0 || N < 0 || K < 1 || !A || !B || !C || lda < (size_t)K || ldb < (size_t)(transb ? K : N) ||
+        ldc < (size_t)N) {
         err = "emulated FP64 product: invalid sizes or pointers";
         return GDFJK_ERR_ARG;
     }
@@ -1822,12 +1823,21 @@ int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb
             cudaMemcpy(tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice);
             tiles_ncb = ncb;
         }
-        const size_t cols = (size_t)N_pad * ngroups;
-        oz_gemm_colexp_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, s>>>(B + c0, ldb, ncc, K, RUN_K, ngroups, N_pad, Eb,
-                                                                              Sb, o->err);
         const size_t units = (size_t)N_pad * nkbt * (MK / 8);
         const int blocks = (int)std::min<size_t>((units + 255) / 256, (size_t)o->num_sms * 16);
-        oz_gemm_split_Bt_kernel<<<blocks, 256, 0, s>>>(B + c0, ldb, ncc, K, N_pad, nkbt, kpg, Eb, Yd);
+        if (transb) {
+            // B is N x K with K contiguous: its rows are split exactly as A's
+            const double* Bc = B + (size_t)c0 * ldb;
+            const size_t warps = (size_t)N_pad * ngroups;
+            oz_gemm_rowexp_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(Bc, ldb, ncc, K, RUN_K, ngroups,
+                                                                                          N_pad, Eb, Sb, o->err);
+            oz_gemm_split_A_kernel<<<blocks, 256, 0, s>>>(Bc, ldb, ncc, K, N_pad, nkbt, kpg, Eb, Yd);
+        } else {
+            const size_t cols = (size_t)N_pad * ngroups;
+            oz_gemm_colexp_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, s>>>(B + c0, ldb, ncc, K, RUN_K, ngroups,
+                                                                                  N_pad, Eb, Sb, o->err);
+            oz_gemm_split_Bt_kernel<<<blocks, 256, 0, s>>>(B + c0, ldb, ncc, K, N_pad, nkbt, kpg, Eb, Yd);
+        }
         CtArgs ca{};
         ca.Xd = Xd;
         ca.Yd = Yd;

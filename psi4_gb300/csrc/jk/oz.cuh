@@ -29,11 +29,12 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
 // Summed device time (ms) of the half-transform kernels of the last build (all batches);
 // valid once that build has completed.
 float oz_last_transform_ms(OzState* o);
-// C (+)= A B to FP64 accuracy from the same digit products (A M x K, B K x N, C M x N, all
-// row-major on the device with leading dimensions lda, ldb, ldc); B is taken in column chunks
-// whose digits fit GDFJK_OZ_GEMM_CHUNK_GB (default 8).  Returns after the product is complete.
+// C (+)= A op(B) to FP64 accuracy from the same digit products (A M x K, C M x N, all
+// row-major on the device with leading dimensions lda, ldb, ldc; op(B) = B, K x N, or with
+// transb op(B) = B^T for B N x K); B is taken in column chunks of op(B) whose digits fit
+// GDFJK_OZ_GEMM_CHUNK_GB (default 8).  Returns after the product is complete.
 int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb, double* C, size_t ldc, int M, int N,
-            int K, int accumulate, cudaStream_t s, std::string& err);
+            int K, int accumulate, cudaStream_t s, std::string& err, int transb = 0);
 // error bits raised by the tensor-core kernels since the last call (0 = none); clears them
 int oz_error_flag(OzState* o, cudaStream_t s);
 

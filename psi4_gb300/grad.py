@@ -36,23 +36,62 @@ def metric_power_frechet(M, W, power=-0.5, condition=1e-10):
     return V @ (Lm * (V.T @ Ws @ V)) @ V.T
 
 
-def two_electron_gradient(ints, df, Gamma, A_raw=None):
-    """Contract Gamma (dE/dB, packed) with derivative integrals through B = M^-1/2 A."""
+def _metric_products_device(engine, Jmhalf, Gamma, A_raw):
+    """G3 = M^-1/2 Gamma and W = Gamma A^T on the tensor cores to FP64 accuracy
+    (gdfjk_gemm_device); W's long inner dimension (the pairs) is taken in chunks whose digits
+    stay within a few GB, accumulated into W.  torch only carries the device buffers."""
+    import torch
+
+    dev = torch.device("cuda", engine.device)
+    naux, npair = Gamma.shape
+    Gd = torch.from_numpy(np.ascontiguousarray(Gamma)).to(dev)
+    Ad = torch.from_numpy(np.ascontiguousarray(A_raw)).to(dev)
+    Jm = torch.from_numpy(np.ascontiguousarray(Jmhalf)).to(dev)
+    G3 = torch.empty_like(Gd)
+    engine.gemm(Jm.data_ptr(), naux, Gd.data_ptr(), npair, G3.data_ptr(), npair, naux, npair, naux)
+    W = torch.empty((naux, naux), dtype=torch.float64, device=dev)
+    kc = max(4096, int(6e9 // (16 * max(naux, 1))))  # 8 BF16 digit slices of a K chunk of Gamma
+    for k0 in range(0, npair, kc):
+        k1 = min(npair, k0 + kc)
+        engine.gemm(Gd[:, k0:].data_ptr(), npair, Ad[:, k0:].data_ptr(), npair, W.data_ptr(), naux, naux, naux, k1 - k0,
+                    transb=True, accumulate=k0 > 0)
+    return G3.cpu().numpy(), W.cpu().numpy()
+
+
+def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None):
+    """Contract Gamma (dE/dB, packed) with derivative integrals through B = M^-1/2 A.  With an
+    engine the two naux^2-sized products with the metric run on its tensor cores (FP64
+    accurate); `timings` (a dict) receives the seconds of each piece."""
+    import time
+
+    t = time.perf_counter()
     if A_raw is None:
         A_raw = ints.three_index(shell_mask=df.sparsity.shell_mask)
         r, c = np.tril_indices(df.nbf)
         A_raw[:, ~df.sparsity.pair_mask[r, c]] = 0.0
-    G3 = df.Jmhalf @ Gamma
-    W = Gamma @ A_raw.T
+    t1 = time.perf_counter()
+    if engine is not None:
+        G3, W = _metric_products_device(engine, df.Jmhalf, Gamma, A_raw)
+    else:
+        G3 = df.Jmhalf @ Gamma
+        W = Gamma @ A_raw.T
+    t2 = time.perf_counter()
     G2 = metric_power_frechet(df.metric, W)
+    t3 = time.perf_counter()
     g3 = ints.three_index_grad(G3, shell_mask=df.sparsity.shell_mask)
+    t4 = time.perf_counter()
     g2 = ints.metric_grad(G2)
+    t5 = time.perf_counter()
+    if timings is not None:
+        timings.update({"three_index_s": t1 - t, "metric_products_s": t2 - t1, "metric_frechet_s": t3 - t2,
+                        "three_index_derivative_contraction_s": t4 - t3, "metric_derivative_contraction_s": t5 - t4,
+                        "metric_products_on": "tensor cores" if engine is not None else "host"})
     return g3 + g2
 
 
-def rhf_gradient(mol, ints, df, scf, Gamma):
+def rhf_gradient(mol, ints, df, scf, Gamma, engine=None, timings=None):
     """Total RHF gradient (natom x 3, Eh/bohr) from a converged SCF and the engine's Gamma
-    for gJ = dE/dJ = 2D, gK = dE/dK = -D."""
+    for gJ = dE/dJ = 2D, gK = dE/dK = -D (the metric products on `engine` when given)."""
     nocc = scf.nocc
     C = scf.C[:, :nocc]
     eps = scf.eps[:nocc]
@@ -62,5 +101,5 @@ def rhf_gradient(mol, ints, df, scf, Gamma):
     g += 2.0 * ints.kinetic_grad(D)
     g += 2.0 * ints.potential_grad(D)
     g -= 2.0 * ints.overlap_grad(W)
-    g += two_electron_gradient(ints, df, Gamma)
+    g += two_electron_gradient(ints, df, Gamma, engine=engine, timings=timings)
     return g

@@ -97,6 +97,14 @@ class DFJKEngine:
                                                         int(ncols), int(ldp), ctypes.c_void_p(out_ptr), int(ldb),
                                                         1 if accumulate else 0))
 
+    def gemm(self, A_ptr: int, lda: int, B_ptr: int, ldb: int, C_ptr: int, ldc: int, M: int, N: int, K: int,
+             transb: bool = False, accumulate: bool = False):
+        """C (+)= A op(B) on the tensor cores to FP64 accuracy (device pointers, row-major;
+        op(B) = B^T with transb, B then N x K)."""
+        self._check(self.L.gdfjk_gemm_device(self.h, 1 if transb else 0, int(M), int(N), int(K), ctypes.c_void_p(A_ptr),
+                                             int(lda), ctypes.c_void_p(B_ptr), int(ldb), ctypes.c_void_p(C_ptr), int(ldc),
+                                             1 if accumulate else 0))
+
     def upload_device_block(self, ptr: int, q0: int, nq: int):
         """Rows q0 .. q0+nq-1 of the packed triangle already in device memory."""
         self._check(self.L.gdfjk_upload_B_device_block(self.h, ctypes.c_void_p(ptr), int(q0), int(nq)))

@@ -53,7 +53,9 @@ def _scf_energy_and_gradient(mol, want_grad):
         C = res.C[:, : res.nocc]
         D = C @ C.T
         _, Gamma = jk.engine.backward(C, 2.0 * D, -D, want_dC=False)
-        g = rhf_gradient(mol, ints, df, res, Gamma)
+        g = rhf_gradient(mol, ints, df, res, Gamma, engine=jk.engine)  # metric products on the tensor cores
+        g_host = rhf_gradient(mol, ints, df, res, Gamma)  # the same products in FP64 on the host
+        assert np.abs(g - g_host).max() < 1e-10
     jk.finalize()
     return res.energy, g
 
@@ -92,4 +94,4 @@ def test_h2o16_gradient_against_central_differences(ints_built, jk_built):
         fd = (Ep - Em) / (2 * h)
         worst = max(worst, abs(g[atom, axis] - fd))
         print(f"(H2O)_16 atom {atom} axis {axis}: analytic {g[atom, axis]: .9f} fd {fd: .9f} diff {g[atom, axis] - fd: .2e}")
-    assert worst < 1e-5
+    assert worst < 1e-6  # the differentiation form's bar (Eh/bohr)

@@ -115,3 +115,35 @@ def test_metric_contract_rejects_bad_leading_dimension(jk_built):
     x = torch.zeros((16, 64), dtype=torch.float64, device=DEV)
     with pytest.raises(GdfjkError, match="leading dimension"):
         eng.metric_contract(x.data_ptr(), x.data_ptr(), 64, x.data_ptr(), ldp=32)
+
+
+@pytest.mark.parametrize("transb", [False, True])
+def test_general_product_both_operand_orders(jk_built, transb):
+    """gdfjk_gemm_device: C (+)= A op(B) for op(B) = B and B^T, sizes off every tile multiple,
+    an inner dimension over several accumulation runs, magnitudes spread over six decades;
+    an inner dimension taken in two accumulated chunks gives the same C (the way the gradient
+    forms Gamma A^T)."""
+    M, N, K = 300, 277, 3100
+    g = torch.Generator(device=DEV)
+    g.manual_seed(17 + int(transb))
+    A = torch.randn((M, K), dtype=torch.float64, device=DEV, generator=g)
+    A *= torch.pow(10.0, torch.rand((M, 1), dtype=torch.float64, device=DEV, generator=g) * 6 - 3)
+    Bm = torch.randn((N, K) if transb else (K, N), dtype=torch.float64, device=DEV, generator=g)
+    opB = Bm.T if transb else Bm
+    ref = A @ opB
+    bound = (A.abs().amax(dim=1, keepdim=True) * opB.abs().amax(dim=0, keepdim=True)) * K ** 0.5
+    eng = DFJKEngine(8, 8, None)
+    C = torch.empty((M, N), dtype=torch.float64, device=DEV)
+    ldb = K if transb else N
+    eng.gemm(A.data_ptr(), K, Bm.data_ptr(), ldb, C.data_ptr(), N, M, N, K, transb=transb)
+    rel = ((C - ref).abs() / bound).max().item()
+    print(f"transb {transb}: max |dC| / (max|row| max|col| sqrt(K)) = {rel:.2e}")
+    assert rel < 1e-13
+    if transb:  # the inner dimension in two chunks, accumulated
+        C2 = torch.empty_like(C)
+        k1 = 1024
+        eng.gemm(A.data_ptr(), K, Bm.data_ptr(), K, C2.data_ptr(), N, M, N, k1, transb=True)
+        eng.gemm(A[:, k1:].data_ptr(), K, Bm[:, k1:].data_ptr(), K, C2.data_ptr(), N, M, N, K - k1, transb=True,
+                 accumulate=True)
+        assert ((C2 - ref).abs() / bound).max().item() < 1e-13
+    eng.close()
