@@ -53,8 +53,8 @@ def _scf_energy_and_gradient(mol, want_grad):
         C = res.C[:, : res.nocc]
         D = C @ C.T
         _, Gamma = jk.engine.backward(C, 2.0 * D, -D, want_dC=False)
-        g = rhf_gradient(mol, ints, df, res, Gamma, engine=jk.engine)  # metric products on the tensor cores
-        g_host = rhf_gradient(mol, ints, df, res, Gamma)  # the same products in FP64 on the host
+        g = rhf_gradient(mol, ints, df, res, Gamma, engine=jk.engine)  # M^-1/2 Gamma on the tensor cores
+        g_host = rhf_gradient(mol, ints, df, res, Gamma)  # the same product in FP64 on the host
         assert np.abs(g - g_host).max() < 1e-10
     jk.finalize()
     return res.energy, g
