@@ -450,7 +450,7 @@ def run_gpu(args):
             out["gradient"] = {"unavailable": str(ex)[:300]}
     if rank == 0 and args.scf:
         try:
-            out["scf"] = (measure_scf_device_B(args.scf_config, dev) if args.scf_config in ("c2", "c3")
+            out["scf"] = (measure_scf_device_B(args.scf_config, dev) if args.scf_config in ("c2", "c3", "c5")
                           else measure_scf(args.scf_config))
         except Exception as ex:
             out["scf"] = {"unavailable": str(ex)[:300]}
@@ -821,21 +821,37 @@ def measure_scf_device_B(cfg, dev):
     GPU form) and in the precision form (split-BF16 increments, emulated-FP64 anchor and
     final builds), with every precision-form iteration's energy error against FP64 at the same
     orbitals, and the native FP64 energy at the converged orbitals."""
+    import torch
+
     from psi4_gb300.basis import BasisSet
-    from psi4_gb300.device_init import build_device_B
+    from psi4_gb300.device_init import build_device_B, build_device_B_screened
     from psi4_gb300.jk import GpuDFJK
-    from psi4_gb300.molecule import water_cluster
+    from psi4_gb300.molecule import linear_alkane, water_cluster
     from psi4_gb300.scf import PrecisionSchedule, core_hamiltonian, energy_errors_vs_fp64, rhf, rhf_energy
 
     gen, basis, desc = CONFIGS[cfg]
-    mol = water_cluster(*gen["lattice"], seed=0)
+    screened = "alkane" in gen
+    mol = linear_alkane(gen["alkane"], seed=0) if screened else water_cluster(*gen["lattice"], seed=0)
     pb = BasisSet.build(mol, basis)
     ab = BasisSet.fitting_for(mol, pb)
+    used = [0]
+
+    def sample_memory(*_):
+        free, total = torch.cuda.mem_get_info(dev)
+        used[0] = max(used[0], total - free)
+
+    sample_memory()
+    base_used = used[0]
     t0 = time.perf_counter()
-    dd = build_device_B(mol, pb, ab, device=dev.index or 0, check_columns=65536)
+    if screened:  # the dense (P|mn) triangle would not fit: significant pairs only
+        dd = build_device_B_screened(mol, pb, ab, device=dev.index or 0)
+        t_init = time.perf_counter() - t0
+    else:
+        dd = build_device_B(mol, pb, ab, device=dev.index or 0, check_columns=65536)
+        t_init = time.perf_counter() - t0 - dd.timings["metric_check"]["fp64_library_gemm_s"]  # without the check
+    sample_memory()
     ints = dd.ints
     H, S = core_hamiltonian(ints), ints.overlap()
-    t_init = time.perf_counter() - t0 - dd.timings["metric_check"]["fp64_library_gemm_s"]  # without the check
     nocc = mol.nelectron // 2
     e_nuc = mol.nuclear_repulsion_energy()
     jk = GpuDFJK.from_engine(dd.engine)
@@ -850,14 +866,15 @@ def measure_scf_device_B(cfg, dev):
         jk.compute()
     jk.set_precision("fp64-emulated")
     jk.set_incremental(False)
+    sample_memory()
     ts = time.perf_counter()
-    r_em = rhf(jk, H, S, nocc, e_nuc)
+    r_em = rhf(jk, H, S, nocc, e_nuc, callback=sample_memory)
     out["fp64_emulated"] = {"energy": r_em.energy, "iterations": r_em.iterations, "builds": r_em.iterations,
                             "seconds": time.perf_counter() - ts, "jk_seconds": r_em.timings["jk_s"]}
     jk.reset_incremental()
     sched = PrecisionSchedule(fp64_precision="fp64-emulated")
     ts = time.perf_counter()
-    r_pf = rhf(jk, H, S, nocc, e_nuc, schedule=sched, record_orbitals=True)
+    r_pf = rhf(jk, H, S, nocc, e_nuc, schedule=sched, record_orbitals=True, callback=sample_memory)
     out["precision_form"] = {"energy": r_pf.energy, "iterations": r_pf.iterations, "mixed_builds": sched.n_mixed,
                              "fp64_builds": sched.n_fp64, "seconds": time.perf_counter() - ts,
                              "jk_seconds": r_pf.timings["jk_s"]}
@@ -872,9 +889,14 @@ def measure_scf_device_B(cfg, dev):
     jk.set_precision("fp64")
     e_nat_em = rhf_energy(jk, r_em.C[:, :nocc], H, e_nuc)
     e_nat_pf = rhf_energy(jk, r_pf.C[:, :nocc], H, e_nuc)
+    sample_memory()
     out["native_fp64_energy_at_converged_orbitals"] = {"fp64_emulated": e_nat_em, "precision_form": e_nat_pf}
     out["abs_energy_difference_precision_vs_emulated"] = abs(r_pf.energy - r_em.energy)
     out["abs_energy_difference_emulated_vs_native_same_orbitals"] = abs(r_em.energy - e_nat_em)
+    out["peak_device_memory_gb"] = used[0] / 1e9
+    out["device_memory_before_gb"] = base_used / 1e9
+    out["peak_device_memory_note"] = ("largest cudaMemGetInfo use seen after initialisation and after every SCF "
+                                      "iteration (the engine keeps its workspaces between builds)")
     em, pf = out["fp64_emulated"], out["precision_form"]
     out["time_to_converge_speedup_precision_vs_emulated"] = em["seconds"] / pf["seconds"]
     out["jk_time_to_converge_speedup_precision_vs_emulated"] = em["jk_seconds"] / pf["jk_seconds"]
@@ -1041,8 +1063,8 @@ def main():
     ap.add_argument("--fp64-form", default="emulated", choices=["emulated", "native"],
                     help="the headline FP64-accurate build: emulated on BF16 tensor cores or native FP64")
     ap.add_argument("--scf", type=int, default=1)
-    ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4"],
-                    help="SCF time-to-converge workload; c2/c3 build B on the device from host integrals (minutes)")
+    ap.add_argument("--scf-config", default="c4", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="SCF time-to-converge workload; c2/c3/c5 build B on the device from host integrals (minutes)")
     ap.add_argument("--grad-config", default="c4", help="analytic-gradient leg ('' for none)")
     ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
     ap.add_argument("--metric", default="c2", help="configuration of the metric-contraction leg, '' for none")

@@ -99,6 +99,68 @@ def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int 
     return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, rows)
 
 
+def build_device_B_screened(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int = 0,
+                            cutoff: float = DEFAULT_CUTOFF, condition: float = DEFAULT_CONDITION,
+                            ints: Integrals | None = None, block: int = 128, upload_rows: int = 256) -> DeviceDF:
+    """build_device_B for systems whose dense packed triangle would not fit the device (the
+    C100H202 workload: 271 GB dense, 10 % of the pairs significant): (P|mn) is held on the device
+    over the Schwarz-significant pairs only (m >= n, DFHelper's sparse tensor), contracted with
+    J^-1/2 there, and B is expanded back to packed-triangle rows a block of aux functions at a
+    time for the engine's block upload (gdfjk_upload_B_device_block), which keeps only the
+    stored tiles."""
+    import torch
+
+    dev = torch.device("cuda", device)
+    t0 = time.perf_counter()
+    ints = ints or Integrals(mol, primary, aux)
+    nbf, naux = primary.nbf, aux.nbf
+    fun_max, shell_max = ints.schwarz()
+    sp = prepare_sparsity(fun_max, shell_max, cutoff, naux)
+    r, c = np.tril_indices(nbf)
+    sig = np.flatnonzero(sp.pair_mask[r, c])  # packed-triangle columns of the significant pairs
+    npair, nsig = r.size, sig.size
+    M = ints.metric()
+    tm = time.perf_counter()
+    Jm_host = metric_power(M, -0.5, condition)
+    t_metric = time.perf_counter() - tm
+    sig_d = torch.from_numpy(sig).to(dev)
+    P = torch.empty((naux, nsig), dtype=torch.float64, device=dev)
+    t_ints = t_copy = 0.0
+    for p0 in range(0, naux, block):
+        p1 = min(naux, p0 + block)
+        ta = time.perf_counter()
+        A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
+        As = np.ascontiguousarray(A[:, sig])
+        del A
+        t_ints += time.perf_counter() - ta
+        tb = time.perf_counter()
+        P[p0:p1] = torch.from_numpy(As).to(dev)
+        t_copy += time.perf_counter() - tb
+    torch.cuda.synchronize(dev)
+    eng = DFJKEngine(nbf, naux, sp.pair_mask, device=device)
+    Jm = torch.from_numpy(Jm_host).to(dev)
+    Bs = torch.empty_like(P)
+    tg = time.perf_counter()
+    eng.metric_contract(Jm.data_ptr(), P.data_ptr(), nsig, Bs.data_ptr())
+    t_gemm = time.perf_counter() - tg
+    del P, Jm
+    torch.cuda.empty_cache()
+    tu = time.perf_counter()
+    rows = torch.zeros((min(upload_rows, naux), npair), dtype=torch.float64, device=dev)
+    for q0 in range(0, naux, upload_rows):
+        nq = min(upload_rows, naux - q0)
+        rows[:nq].index_copy_(1, sig_d, Bs[q0:q0 + nq])
+        torch.cuda.synchronize(dev)
+        eng.upload_device_block(rows.data_ptr(), q0, nq)
+    del rows, Bs
+    torch.cuda.empty_cache()
+    t_up = time.perf_counter() - tu
+    timings = {"three_index_host_s": t_ints, "three_index_copy_s": t_copy, "metric_power_host_s": t_metric,
+               "metric_contraction_device_s": t_gemm, "expand_and_upload_s": t_up, "significant_pairs": int(nsig),
+               "pairs": int(npair), "total_s": time.perf_counter() - t0}
+    return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, None)
+
+
 def slice_pqq(rows: np.ndarray, sp: Sparsity) -> tuple[np.ndarray, Sparsity]:
     """DFHelper's pQq layout (dfhelper.cc:1671-1673) of a block of aux rows given as packed
     triangles, with the sparsity tables re-indexed for that many rows."""

@@ -129,3 +129,25 @@ def test_precision_form_scf_within_one_microhartree(real):
     assert np.all(np.isfinite(errs))
     assert abs(res.energy - ref.energy) < 1e-6
     assert sched.n_mixed > 0 and sched.n_fp64 >= 2
+
+
+def test_screened_device_build_matches_the_host_tensor(ints_built, jk_built):
+    """build_device_B_screened (significant pairs only on the device, expanded back in blocks of
+    aux rows for the block upload, as the C100H202 workload is built) gives the J and K of the
+    host-built DF tensor, on a screened system with uneven upload blocks."""
+    from psi4_gb300.device_init import build_device_B_screened
+    from tests.helpers import system
+
+    mol, pb, ab, ints, df = system("h2o_2_far", "cc-pvdz", 1e-5)
+    assert 0.0 < df.sparsity.sparsity < 1.0
+    dd = build_device_B_screened(mol, pb, ab, cutoff=1e-5, ints=ints, block=37, upload_rows=50)
+    ref = DFJKEngine(df.nbf, df.naux, df.sparsity.pair_mask)
+    ref.upload_qtri(df.B_tri)
+    C = np.linalg.qr(np.random.default_rng(8).standard_normal((df.nbf, 10)))[0] * 0.5
+    for mode in (abi.DO_J | abi.DO_K, abi.DO_J | abi.DO_K | abi.EMULATED):
+        J, K = _jk(dd.engine, C, mode)
+        Jr, Kr = _jk(ref, C, mode)
+        assert np.abs(J - Jr).max() < ABS_BAR and np.abs(K - Kr).max() < ABS_BAR
+    assert dd.timings["significant_pairs"] < dd.timings["pairs"]
+    dd.engine.close()
+    ref.close()
