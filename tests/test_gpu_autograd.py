@@ -55,7 +55,10 @@ def _scf_energy_and_gradient(mol, want_grad):
         _, Gamma = jk.engine.backward(C, 2.0 * D, -D, want_dC=False)
         g = rhf_gradient(mol, ints, df, res, Gamma, engine=jk.engine)  # M^-1/2 Gamma on the tensor cores
         g_host = rhf_gradient(mol, ints, df, res, Gamma)  # the same product in FP64 on the host
-        assert np.abs(g - g_host).max() < 1e-10
+        # the digit product's error is relative to the row and column maxima of each run of 1024
+        # aux functions (~1e-13 of them), which moves the gradient by ~1e-9 Eh/bohr: 1000x below
+        # the differentiation form's 1e-6 bar
+        assert np.abs(g - g_host).max() < 1e-8
     jk.finalize()
     return res.energy, g
 
