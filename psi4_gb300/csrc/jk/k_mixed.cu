@@ -482,9 +482,11 @@ void mixed_destroy(MixedState* m) {
 
 void mixed_release(MixedState* m) {
     if (!m) return;
-    big_free(m->Bh);
-    big_free(m->Bl);
-    m->Bh = m->Bl = nullptr;
+    void* ps[] = {m->Bh, m->Bl, m->Uh, m->Ul, m->Xh, m->Xl, m->part};
+    for (void* p : ps) big_free(p);
+    m->Bh = m->Bl = m->Uh = m->Ul = m->Xh = m->Xl = nullptr;
+    m->part = nullptr;
+    m->U_cap = m->X_cap = m->part_cap = 0;
     m->B_ready = false;
 }
 

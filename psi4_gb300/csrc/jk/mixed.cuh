@@ -14,8 +14,8 @@ MixedState* mixed_create();
 void mixed_destroy(MixedState* m);
 // B changed: drop the split copies and the incremental history.
 void mixed_invalidate(MixedState* m);
-// Memory pressure: drop the split copies of B (rebuilt on next use) but keep the incremental
-// history, which is still valid for the same B.
+// Memory pressure: drop the split copies of B and the factor / X workspaces (rebuilt on next
+// use) but keep the incremental history, which is still valid for the same B.
 void mixed_release(MixedState* m);
 size_t mixed_query_memory(int nbf, int naux, int max_nocc);
 // K for the lr-symmetric density C C^T (C padded, device), written to K (nbf x nbf, device).
