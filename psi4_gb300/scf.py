@@ -157,16 +157,82 @@ class PrecisionSchedule:
         return self.fp64_streak >= 2
 
 
+def sad_guess(mol, basis: str, maxiter: int = 60, conv: float = 1e-8) -> np.ndarray:
+    """psi4's default SCF guess, superposition of atomic densities (libscf_solver/sad.cc): one
+    spin-averaged SCF per element in its own basis (fractional occupation of the open shell,
+    spread evenly over its degenerate orbitals; J and K from the atom's density-fitted
+    integrals), the molecular alpha density the block-diagonal sum of the atomic ones over
+    psi4's atom-by-atom function order.  Returns a factor Cs (nbf x k) with Cs Cs^T that
+    density (each atomic natural orbital scaled by the square root of half its occupation),
+    ready to be pushed into a JK object like occupied orbitals."""
+    from .basis import BasisSet
+    from .dfhelper import build_df_tensor
+    from .ints import Integrals
+    from .molecule import Molecule
+
+    factors = {}
+    for sym in dict.fromkeys(mol.symbols):
+        amol = Molecule([sym], np.zeros((1, 3)))
+        pb = BasisSet.build(amol, basis)
+        ab = BasisSet.fitting_for(amol, pb)
+        ints = Integrals(amol, pb, ab)
+        B = build_df_tensor(amol, pb, ab, ints=ints).dense()  # (naux, n, n), a few hundred KB
+        Ha, Sa = core_hamiltonian(ints), ints.overlap()
+        Xa = orthogonalizer(Sa)
+        nel = float(amol.nelectron)
+        D = np.zeros_like(Ha)
+        Dold = None
+        for _ in range(maxiter):
+            J = np.einsum("qmn,q->mn", B, np.einsum("qls,ls->q", B, D))
+            K = np.einsum("qml,ls,qsn->mn", B, D, B)
+            F = Ha + J - 0.5 * K  # spin-averaged closed-shell form of the total density D
+            eps, Cp = np.linalg.eigh(Xa.T @ F @ Xa)
+            Ca = Xa @ Cp
+            occ = np.zeros(eps.size)
+            left, i = nel, 0
+            while left > 1e-12 and i < eps.size:
+                deg = np.flatnonzero(np.abs(eps - eps[i]) < 1e-4)
+                deg = deg[deg >= i]
+                take = min(left, 2.0 * deg.size)
+                occ[deg] = take / deg.size
+                left -= take
+                i = deg[-1] + 1
+            Dn = (Ca * occ) @ Ca.T
+            D = Dn if Dold is None else 0.5 * (Dn + Dold)
+            if Dold is not None and np.abs(D - Dold).max() < conv:
+                break
+            Dold = D
+        keep = occ > 0
+        factors[sym] = Ca[:, keep] * np.sqrt(occ[keep] / 2.0)  # alpha density = D / 2
+    blocks, nbf_atoms = [], []
+    for sym in mol.symbols:
+        blocks.append(factors[sym])
+        nbf_atoms.append(factors[sym].shape[0])
+    nbf, k = sum(nbf_atoms), sum(b.shape[1] for b in blocks)
+    Cs = np.zeros((nbf, k))
+    r = c = 0
+    for blk in blocks:
+        Cs[r:r + blk.shape[0], c:c + blk.shape[1]] = blk
+        r += blk.shape[0]
+        c += blk.shape[1]
+    return Cs
+
+
 def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=None, diis_start=1,
         fail_on_maxiter=True, callback=None, verbose=False, schedule: PrecisionSchedule | None = None,
-        record_orbitals=False) -> SCFResult:
+        record_orbitals=False, guess_density_factor=None) -> SCFResult:
     """Run RHF with a JK object exposing C_clear/C_left_add/compute/J/K.  With a
     PrecisionSchedule the JK switches between the mixed and FP64 forms per iteration.
     `record_orbitals` keeps every iteration's occupied orbitals in ``result.orbitals`` (for
-    evaluating afterwards the FP64 energy at each iterate: `energy_errors_vs_fp64`)."""
+    evaluating afterwards the FP64 energy at each iterate: `energy_errors_vs_fp64`).
+    `guess_density_factor` (e.g. `sad_guess`): the first Fock build is made from that density
+    instead of the core guess's orbitals, as psi4 does with its SAD guess."""
     X = orthogonalizer(S)
     t0 = time.perf_counter()
-    if guess_C is None:
+    if guess_density_factor is not None:
+        C = np.ascontiguousarray(guess_density_factor)
+        eps = np.zeros(C.shape[1])
+    elif guess_C is None:
         # core guess
         eps, Cp = np.linalg.eigh(X.T @ H @ X)
         C = X @ Cp
@@ -183,7 +249,7 @@ def rhf(jk, H, S, nocc, e_nuc, e_conv=1e-10, d_conv=1e-8, maxiter=100, guess_C=N
     F = J = K = D = None
     orbitals = []
     for it in range(1, maxiter + 1):
-        Cocc = np.ascontiguousarray(C[:, :nocc])
+        Cocc = np.ascontiguousarray(C if (it == 1 and guess_density_factor is not None) else C[:, :nocc])
         if record_orbitals:
             orbitals.append(Cocc)
         D = Cocc @ Cocc.T
