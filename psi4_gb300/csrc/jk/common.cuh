@@ -25,6 +25,27 @@ constexpr int TILE_ELEMS = TILE * TILE;
 constexpr int DEV_ERR_INDEX = 1;
 constexpr int DEV_ERR_WAIT = 2;
 
+// Bounds-checked build (-DGDFJK_BOUNDS_CHECK, `_native.build_jk(bounds_check=True)`): the
+// kernels check every bulk-copy source range and global write index against the extent of
+// its buffer; a violation raises DEV_ERR_INDEX, prints the first few (code, index, limit)
+// triples and skips the access (a producer stops its stream of copies and aborts its block).
+// Compiled out otherwise (BCHK is then `true`).
+#ifdef GDFJK_BOUNDS_CHECK
+static __device__ int g_bounds_reports;  // per translation unit: the first 16 violations are printed
+__device__ __forceinline__ bool bounds_check(bool ok, int* err, int code, long long idx, long long lim) {
+    if (!ok) {
+        atomicOr(err, DEV_ERR_INDEX);
+        if (atomicAdd(&g_bounds_reports, 1) < 16)
+            printf("GDFJK_BOUNDS code %d block %d thread %d index %lld limit %lld\n", code, (int)blockIdx.x,
+                   (int)threadIdx.x, idx, lim);
+    }
+    return ok;
+}
+#define BCHK(cond, err, code, idx, lim) ::gdfjk::bounds_check((cond), (err), (code), (long long)(idx), (long long)(lim))
+#else
+#define BCHK(cond, err, code, idx, lim) true
+#endif
+
 struct TileLayout {
     int nT;          // tiles per dimension
     int ntiles;      // stored tiles

@@ -1266,7 +1266,7 @@ struct OzState {
     size_t C_cap = 0, sc_cap = 0;
     float2* Xdf = nullptr;
     __nv_bfloat16* Xd = nullptr;
-    size_t X_cap = 0;  // aux functions per batch the X buffers hold
+    size_t X_cap = 0;  // (aux function, occupied column) pairs the X buffers hold: qb * nocc_p
     unsigned* xmax = nullptr;
     float* Sx = nullptr;
     size_t xm_cap = 0, sx_cap = 0;
@@ -1291,7 +1291,7 @@ struct OzState {
     __nv_bfloat16* Cd_r = nullptr;
     size_t Cr_cap = 0, scr_cap = 0;
     __nv_bfloat16* Xd_r = nullptr;
-    size_t Xr_cap = 0;
+    size_t Xr_cap = 0;  // the same for the right factor's digits
     float* Sx_r = nullptr;
     size_t sxr_cap = 0;
     int2* d_tiles_all = nullptr;
@@ -1539,12 +1539,15 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
     const double per_q = (double)nocc_p * ((double)nbf * 8.0 + (nonsym ? 2.0 : 1.0) * (double)nbf_p * NSL * 2.0);
     int qb = (int)std::min<double>((double)naux, std::max<double>(G, std::floor(x_cap_bytes() / per_q / G) * G));
     qb = std::max(1, qb);
-    if ((size_t)qb > o->X_cap) {
+    // capacity in (aux function, column) pairs, not in aux functions: a later build with more
+    // occupied columns gets a smaller batch whose buffers may still need to be larger
+    const size_t x_need = (size_t)qb * nocc_p;
+    if (x_need > o->X_cap) {
         o->X_cap = 0;
-        if ((rc = oz_alloc((void**)&o->Xdf, (size_t)nbf * qb * nocc_p * 8, err)) ||
-            (rc = oz_alloc((void**)&o->Xd, (size_t)nbf_p * qb * nocc_p * NSL * 2, err)))
+        if ((rc = oz_alloc((void**)&o->Xdf, (size_t)nbf * x_need * 8, err)) ||
+            (rc = oz_alloc((void**)&o->Xd, (size_t)nbf_p * x_need * NSL * 2, err)))
             return rc;
-        o->X_cap = qb;
+        o->X_cap = x_need;
     }
     const int ngroups_max = (qb + G - 1) / G;
     if ((size_t)nbf * ngroups_max > o->xm_cap) {
@@ -1558,10 +1561,10 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         o->sx_cap = (size_t)nbf_p * ngroups_max;
     }
     if (nonsym) {
-        if ((size_t)qb > o->Xr_cap) {
+        if (x_need > o->Xr_cap) {
             o->Xr_cap = 0;
-            if ((rc = oz_alloc((void**)&o->Xd_r, (size_t)nbf_p * qb * nocc_p * NSL * 2, err))) return rc;
-            o->Xr_cap = qb;
+            if ((rc = oz_alloc((void**)&o->Xd_r, (size_t)nbf_p * x_need * NSL * 2, err))) return rc;
+            o->Xr_cap = x_need;
         }
         if ((size_t)nbf_p * ngroups_max > o->sxr_cap) {
             o->sxr_cap = 0;

@@ -236,3 +236,34 @@ def test_emulated_rejects_wide_occupation(jk_built):
         eng.compute(C, mode=abi.DO_K | abi.EMULATED)
     _, K, _ = eng.compute(C, mode=abi.DO_K)  # the engine stays usable
     assert np.isfinite(K).all()
+
+
+@pytest.mark.parametrize("nocc", [401, 702])
+def test_emulated_wide_factors(ints_built, jk_built, nocc):
+    """Factors wider than the basis (as the SAD guess's natural orbitals of a large molecule
+    are: 702 columns for C100H202): the emulated K against native FP64 with one aux function
+    per contraction group (nocc_pad 704) or two (416)."""
+    mol, pb, ab, ints, df = system("h2o_8")
+    eng = _engine(df)
+    C = np.random.default_rng(nocc).standard_normal((df.nbf, nocc)) * 0.05
+    _, Kn, _ = eng.compute(C, mode=abi.DO_J | abi.DO_K)
+    _, Ke, _ = eng.compute(C, mode=EMU)
+    err = np.abs(Ke - Kn).max()
+    print(f"nocc {nocc}: max|K| {np.abs(Kn).max():.3e} max|dK| {err:.2e}")
+    assert err < _random_bound(Kn)
+    eng.close()
+
+
+def test_emulated_batch_buffers_follow_the_column_count(ints_built, jk_built, monkeypatch):
+    """A build with more occupied columns after one with fewer, on one engine, where the second
+    gets a smaller aux batch (qb 5 against 8) that still needs larger X buffers (5 x 704 > 8 x
+    416 column pairs): the buffers grow, and both builds agree with native FP64."""
+    mol, pb, ab, ints, df = system("h2o_8")
+    eng = _engine(df)
+    monkeypatch.setenv("GDFJK_OZ_XCAP_GB", "0.02")
+    for nocc in (401, 702):
+        C = np.random.default_rng(nocc + 1).standard_normal((df.nbf, nocc)) * 0.05
+        _, Kn, _ = eng.compute(C, mode=abi.DO_J | abi.DO_K)
+        _, Ke, _ = eng.compute(C, mode=EMU)
+        assert np.abs(Ke - Kn).max() < _random_bound(Kn)
+    eng.close()
