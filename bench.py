@@ -889,14 +889,17 @@ def measure_scf_device_B(cfg, dev):
         {"iter": e["iter"], "precision": e.get("precision"), "error": e["energy_error_vs_fp64"]} for e in r_pf.log]
     out["precision_form"]["max_abs_energy_error_mixed_iterations"] = max(
         [abs(e["energy_error_vs_fp64"]) for e in r_pf.log if e.get("precision") == "mixed"] or [0.0])
-    # the native FP64 energy at both converged orbital sets (one FP64-pipe build each)
-    jk.set_precision("fp64")
-    e_nat_em = rhf_energy(jk, r_em.C[:, :nocc], H, e_nuc)
-    e_nat_pf = rhf_energy(jk, r_pf.C[:, :nocc], H, e_nuc)
-    sample_memory()
-    out["native_fp64_energy_at_converged_orbitals"] = {"fp64_emulated": e_nat_em, "precision_form": e_nat_pf}
     out["abs_energy_difference_precision_vs_emulated"] = abs(r_pf.energy - r_em.energy)
-    out["abs_energy_difference_emulated_vs_native_same_orbitals"] = abs(r_em.energy - e_nat_em)
+    sample_memory()
+    try:
+        # the native FP64 energy at both converged orbital sets (one FP64-pipe build each)
+        jk.set_precision("fp64")
+        e_nat_em = rhf_energy(jk, r_em.C[:, :nocc], H, e_nuc)
+        e_nat_pf = rhf_energy(jk, r_pf.C[:, :nocc], H, e_nuc)
+        out["native_fp64_energy_at_converged_orbitals"] = {"fp64_emulated": e_nat_em, "precision_form": e_nat_pf}
+        out["abs_energy_difference_emulated_vs_native_same_orbitals"] = abs(r_em.energy - e_nat_em)
+    except Exception as ex:  # reported, not hidden
+        out["native_fp64_energy_at_converged_orbitals"] = {"unavailable": str(ex)[:300]}
     out["peak_device_memory_gb"] = used[0] / 1e9
     out["device_memory_before_gb"] = base_used / 1e9
     out["peak_device_memory_note"] = ("largest cudaMemGetInfo use seen after initialisation and after every SCF "

@@ -242,6 +242,12 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
     if (mode & GDFJK_DO_K) h->last_emulated = false;
     const bool native_k = do_K && nocc > 0 && !(mode & GDFJK_MIXED) && !(mode & GDFJK_EMULATED);
     int rc = ensure_workspace(h, nocc_pad, nonsym, native_k);
+    if (rc == GDFJK_ERR_OOM && native_k) {  // the FP64 X workspace: give both tensor-core forms' copies back, retry
+        CK(cudaStreamSynchronize(h->stream));
+        mixed_release(h->mixed);
+        oz_release(h->oz);
+        rc = ensure_workspace(h, nocc_pad, nonsym, native_k);
+    }
     if (rc) return rc;
     cudaStream_t s = h->stream;
     TileLayout L = layout_of(h);
@@ -885,6 +891,12 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
     const int nbf = h->nbf, nbf_pad = h->nbf_pad, naux = h->naux;
     const int nocc_pad = round_up(std::max(nocc, 0), 32);
     int rc = ensure_workspace(h, std::max(nocc_pad, 32), false, true);
+    if (rc == GDFJK_ERR_OOM) {  // as the native K: release the tensor-core forms' copies of B, retry once
+        CK(cudaStreamSynchronize(s));
+        mixed_release(h->mixed);
+        oz_release(h->oz);
+        rc = ensure_workspace(h, std::max(nocc_pad, 32), false, true);
+    }
     if (rc) return rc;
     size_t np2 = (size_t)nbf_pad * nbf_pad, n2 = (size_t)nbf * nbf;
     size_t npair = (size_t)nbf * (nbf + 1) / 2;
