@@ -2,6 +2,11 @@
 
 * ``libgdfints.so`` — host integral provider (C++/OpenMP, g++), include/gdfints.h.
 * ``libgdfjk.so``   — the GB300 DF-JK engine (CUDA for sm_103a + C++ host), include/gdfjk.h.
+* ``libgdfjk_bchk.so`` — the same engine compiled with -DGDFJK_BOUNDS_CHECK: every bulk-copy
+  source range and global write of the tensor-core kernels is checked against its buffer's
+  extent (a violation sets the device error flag, GDFJK_ERR_DEVICE, instead of faulting).
+  Built on request (``build_jk(bounds_check=True)``) and loaded instead of libgdfjk.so when
+  GDFJK_BOUNDS_CHECK=1 is set in the environment before the first load.
 
 Both are compiled into ``psi4_gb300/lib/`` (git-ignored).  Loading never falls back to
 anything else: a missing library raises.
@@ -23,6 +28,7 @@ CSRC = os.path.join(PKG, "csrc")
 
 INTS_SO = os.path.join(LIB, "libgdfints.so")
 JK_SO = os.path.join(LIB, "libgdfjk.so")
+JK_BCHK_SO = os.path.join(LIB, "libgdfjk_bchk.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 JK_SOURCES = ["gdfjk_host.cu", "j_kernels.cu", "k_fp64.cu", "k_mixed.cu", "k_oz.cu", "backward.cu", "noalloc.cu"]
@@ -47,7 +53,8 @@ def _run(cmd):
 def build_ints(force: bool = False) -> str:
     os.makedirs(LIB, exist_ok=True)
     src = os.path.join(CSRC, "ints", "gdf_ints.cpp")
-    if force or not os.path.exists(INTS_SO) or os.path.getmtime(INTS_SO) < os.path.getmtime(src):
+    newest = max(os.path.getmtime(p) for p in (src, os.path.join(CSRC, "ints", "gto_tables.h")))
+    if force or not os.path.exists(INTS_SO) or os.path.getmtime(INTS_SO) < newest:
         _run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-I", INC, "-o", INTS_SO + ".tmp", src])
         os.replace(INTS_SO + ".tmp", INTS_SO)
     return INTS_SO
@@ -57,18 +64,24 @@ def _jk_sources():
     return [os.path.join(CSRC, "jk", s) for s in JK_SOURCES if os.path.exists(os.path.join(CSRC, "jk", s))]
 
 
-def build_jk(force: bool = False, extra_flags=None) -> str:
+def build_jk(force: bool = False, extra_flags=None, bounds_check: bool = False) -> str:
+    """Compile libgdfjk.so (or, with `bounds_check`, libgdfjk_bchk.so) unless it is newer than
+    every source and header."""
     os.makedirs(LIB, exist_ok=True)
+    out = JK_BCHK_SO if bounds_check else JK_SO
     srcs = _jk_sources()
     hdrs = [os.path.join(CSRC, "jk", h) for h in os.listdir(os.path.join(CSRC, "jk")) if h.endswith((".cuh", ".h"))]
     hdrs.append(os.path.join(INC, "gdfjk.h"))
+    hdrs.append(os.path.join(CSRC, "ints", "gto_tables.h"))
     newest = max(os.path.getmtime(p) for p in srcs + hdrs)
-    if not force and os.path.exists(JK_SO) and os.path.getmtime(JK_SO) >= newest:
-        return JK_SO
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
     nvcc = _nvcc()
-    objdir = os.path.join(LIB, "obj")
+    objdir = os.path.join(LIB, "obj_bchk" if bounds_check else "obj")
     os.makedirs(objdir, exist_ok=True)
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "--expt-relaxed-constexpr"]
+    if bounds_check:
+        flags.append("-DGDFJK_BOUNDS_CHECK")
     flags += list(extra_flags or [])
 
     def compile_one(src):
@@ -78,9 +91,9 @@ def build_jk(force: bool = False, extra_flags=None) -> str:
 
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    _run([nvcc] + ARCH + ["-shared", "-o", JK_SO + ".tmp"] + objs)
-    os.replace(JK_SO + ".tmp", JK_SO)
-    return JK_SO
+    _run([nvcc] + ARCH + ["-shared", "-o", out + ".tmp"] + objs)
+    os.replace(out + ".tmp", out)
+    return out
 
 
 _ints = None
@@ -99,15 +112,17 @@ def ints_lib() -> ctypes.CDLL:
 
 
 def jk_lib() -> ctypes.CDLL:
-    """Load libgdfjk.so.  Raises if it has not been built: there is no other JK path."""
+    """Load libgdfjk.so (libgdfjk_bchk.so when GDFJK_BOUNDS_CHECK=1).  Raises if it has not
+    been built: there is no other JK path."""
     global _jk
     with _lock:
         if _jk is None:
-            if not os.path.exists(JK_SO):
-                raise RuntimeError(
-                    f"{JK_SO} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
-                )
-            _jk = ctypes.CDLL(JK_SO)
+            checked = os.environ.get("GDFJK_BOUNDS_CHECK", "0") == "1"
+            path = JK_BCHK_SO if checked else JK_SO
+            if not os.path.exists(path):
+                how = "_native.build_jk(bounds_check=True)" if checked else "import __graft_entry__ as g; g.build()"
+                raise RuntimeError(f"{path} is missing: build it with `python -c '{how}'`")
+            _jk = ctypes.CDLL(path)
             _declare_jk(_jk)
         return _jk
 

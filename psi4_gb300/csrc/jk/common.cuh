@@ -45,6 +45,30 @@ __device__ __forceinline__ bool bounds_check(bool ok, int* err, int code, long l
 #else
 #define BCHK(cond, err, code, idx, lim) true
 #endif
+// [off, off + len) inside [0, lim) (elements or bytes, as the limit is counted)
+#define BRANGE(off, len, lim, err, code) \
+    BCHK((size_t)(off) + (size_t)(len) <= (size_t)(lim), err, code, (size_t)(off) + (size_t)(len), lim)
+
+// Codes of the checked sites (printed with the offending index and its limit).
+enum BoundsSite {
+    BC_TR_LIST = 10,   // emulated half-transform: listed k-block position
+    BC_TR_BD = 11,     //   bulk copy of the int8 digits of B
+    BC_TR_CD = 12,     //   bulk copy of the BF16 digits of C^T
+    BC_TR_X = 13,      //   epilogue: X element
+    BC_TR_XMAX = 14,   //   epilogue: group maximum of X
+    BC_TR_SA = 15,     //   epilogue: row weight of B
+    BC_SX_READ = 20,   // split of X: X read
+    BC_SX_WRITE = 21,  //   digit slices written
+    BC_SX_SX = 22,     //   group weights
+    BC_CT_A = 30,      // emulated contraction: bulk copy of the row operand
+    BC_CT_B = 31,      //   bulk copy of the column operand
+    BC_CT_S = 32,      //   row / column weights
+    BC_CT_OUT = 33,    //   output tile or partial tile
+    BC_RED = 40,       // reduction of partial tiles (both forms): tile map and partial reads
+    BC_MX_A = 50,      // split-precision GEMM: bulk copy of the A operand
+    BC_MX_B = 51,      //   bulk copy of the B operand
+    BC_MX_OUT = 52,    //   epilogue write (X blocks or partial tiles)
+};
 
 struct TileLayout {
     int nT;          // tiles per dimension

@@ -73,6 +73,8 @@ struct TcArgs {
     const int* mb_ptr;
     const int* mb_kb;
     int nnz, nmb;
+    // extents in elements (checked in the bounds-checked build)
+    size_t lim_Bs, lim_Ut, lim_X, lim_part;
 };
 
 __device__ __forceinline__ uint32_t pack_bf162(float a, float b) {
@@ -178,6 +180,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
             const size_t stepc1 = (MODE == MODE_CONTRACT && (b_row / MM) + 1 < a.nbf_p / MM) ? blkA : 0;
             for (int kb = 0; kb < nkb; ++kb, ++kg) {
                 if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) break;
+                bool in_range = true;
+                if (MODE == MODE_TRANSFORM)
+                    in_range = BCHK(kb0 + kb < a.nnz, a.err, BC_MX_A, kb0 + kb, a.nnz) &&
+                               BRANGE(pah - a.Bsh, blkA, a.lim_Bs, a.err, BC_MX_A) &&
+                               BRANGE((pbh - a.Uth) + (size_t)a.mb_kb[kb0 + kb] * stepb, (size_t)N * MK, a.lim_Ut, a.err,
+                                      BC_MX_B);
+                else
+                    in_range = BRANGE(pah - a.Xhi, blkA, a.lim_X, a.err, BC_MX_A) &&
+                               (stepc0 == 0 || BRANGE(pbh - a.Xhi, blkA, a.lim_X, a.err, BC_MX_B)) &&
+                               (stepc1 == 0 || BRANGE(pch - a.Xhi, blkA, a.lim_X, a.err, BC_MX_B));
+                if (!in_range) {
+                    *abort_flag = 1;  // the consumers leave their waits; no copy of this stage was issued
+                    break;
+                }
                 uint8_t* st = smem + (size_t)s * stage_bytes;
                 tc::mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
                 tc::bulk_load(st, pah, A_TILE_BYTES, &full[s]);
@@ -300,6 +316,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
                     size_t blk = (rowblk + k0 / MK) * (size_t)(MM * MK);  // elements
                     uint32_t ch = (uint32_t)((k0 % MK) / 8);
                     uint32_t o0 = tc::swz_offset(rr, ch) / 2, o1 = tc::swz_offset(rr, ch + 1) / 2;
+                    if (!BRANGE(blk, (size_t)MM * MK, a.lim_X, a.err, BC_MX_OUT)) continue;
                     *reinterpret_cast<uint4*>(a.Xhi + blk + o0) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
                     *reinterpret_cast<uint4*>(a.Xhi + blk + o1) = make_uint4(hi[4], hi[5], hi[6], hi[7]);
                     *reinterpret_cast<uint4*>(a.Xlo + blk + o0) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
@@ -307,9 +324,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(const TcArgs a) 
                 }
             } else {
                 float* dst = a.part + (((size_t)split * a.ntiles_out + tile) * MM + r) * CN;
+                const bool wok = BRANGE(dst - a.part, CN, a.lim_part, a.err, BC_MX_OUT);
                 for (int c0 = 0; c0 < CN; c0 += 16) {
                     uint32_t v[16];
-                    tc::tmem_ld16(cbase + (uint32_t)c0, v);
+                    tc::tmem_ld16(cbase + (uint32_t)c0, v);  // warp-collective: every lane loads
+                    if (!wok) continue;
                     float4* d4 = reinterpret_cast<float4*>(dst + c0);
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
@@ -395,7 +414,8 @@ __global__ void split_Ut_kernel(const double* __restrict__ U, int ldu, int nbf, 
 // tiles; `tile_of_block[I * ncb + Jc]` maps a (row block, column block) to its tile index.
 __global__ void reduce_mixed_kernel(const float* __restrict__ part, int nsplit, int ntiles_out, int nbf,
                                     const int* __restrict__ tile_of_block, int ncb, double* __restrict__ K, int ldk,
-                                    double* __restrict__ Kacc, int accumulate) {
+                                    double* __restrict__ Kacc, int accumulate, size_t lim_part,
+                                    int* __restrict__ err) {
     size_t n_lower = (size_t)nbf * (nbf + 1) / 2;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n_lower; p += (size_t)gridDim.x * blockDim.x) {
         size_t m = (size_t)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
@@ -405,6 +425,9 @@ __global__ void reduce_mixed_kernel(const float* __restrict__ part, int nsplit, 
         int I = (int)(m / MM), Jc = (int)(n / CN);
         int t = tile_of_block[I * ncb + Jc];
         size_t off = ((size_t)t * MM + (m % MM)) * CN + (n % CN);
+        if (!BCHK(t >= 0, err, BC_RED, t, ntiles_out) ||
+            !BRANGE((size_t)(nsplit - 1) * ntiles_out * MM * CN + off, 1, lim_part, err, BC_RED))
+            continue;
         double s = 0.0;
         for (int k = 0; k < nsplit; ++k) s += (double)part[(size_t)k * ntiles_out * MM * CN + off];
         if (accumulate) s += Kacc[m * nbf + n];
@@ -622,6 +645,9 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
         ta.nbuf = (2 * ta.n_cols <= 512) ? 2 : 1;
         ta.tmem_cols = pow2_cols(ta.nbuf * ta.n_cols);
         ta.n_items = ta.n_mtiles;
+        ta.lim_Bs = (size_t)naux * m->nnz * (MM * MK);
+        ta.lim_Ut = m->U_cap;
+        ta.lim_X = m->X_cap;
         unsigned grid = (unsigned)std::min(ta.n_items, m->num_sms);
         tc_gemm_kernel<MODE_TRANSFORM><<<grid, TC_THREADS, SMEM_BUDGET, s>>>(ta);
     }
@@ -681,6 +707,8 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
     ca.nbuf = 2;
     ca.tmem_cols = pow2_cols(2 * CN);
     ca.n_items = ntiles_out * nsplit;
+    ca.lim_X = m->X_cap;
+    ca.lim_part = m->part_cap;
     unsigned cgrid = (unsigned)std::min(ca.n_items, m->num_sms);
     tc_gemm_kernel<MODE_CONTRACT><<<cgrid, TC_THREADS, SMEM_BUDGET, s>>>(ca);
     // ---- fixed-order FP64 reduction (+ running K for incremental builds)
@@ -697,7 +725,7 @@ int mixed_k_factor(MixedState* m, const double* B, const TileLayout& L, const in
         size_t nl = (size_t)nbf * (nbf + 1) / 2;
         int blocks = (int)std::min<size_t>((nl + 255) / 256, (size_t)m->num_sms * 16);
         reduce_mixed_kernel<<<blocks, 256, 0, s>>>(m->part, nsplit, ntiles_out, nbf, m->d_tile_of_block, m->ncb, K, nbf,
-                                                   m->Kacc, acc);
+                                                   m->Kacc, acc, m->part_cap, m->err);
     }
     m->have_prev = true;
     cudaError_t e = cudaGetLastError();

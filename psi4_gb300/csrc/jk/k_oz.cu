@@ -391,6 +391,9 @@ struct TrArgs {
     size_t kdim_b;
     int stages, nbuf, n_items, ncols;
     int* err;
+    // extents of the buffers (checked in the bounds-checked build): Bd in bytes, the rest in
+    // elements
+    size_t lim_Bd, lim_Cd, lim_X, lim_xmax, lim_sA;
 };
 
 // The half-transform keeps its A operand (the digit slices of B) in tensor memory: the
@@ -601,6 +604,14 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                     ok = false;
                     break;
                 }
+                if (!BCHK(p0 + p < a.nnz, a.err, BC_TR_LIST, p0 + p, a.nnz) ||
+                    !BRANGE(((size_t)Q * a.nnz + p0 + p) * I8_BLOCK, I8_BLOCK, a.lim_Bd, a.err, BC_TR_BD) ||
+                    !BRANGE(((size_t)chunk * a.nkb + a.mb_kb[p0 + p]) * NSL * N * MK, (size_t)NSL * N * MK, a.lim_Cd,
+                            a.err, BC_TR_CD)) {
+                    *abort_flag = 1;  // the consumers leave their waits; no copy of this stage was issued
+                    ok = false;
+                    break;
+                }
                 uint8_t* st = smem + (size_t)s * stage_bytes;
                 tc::mbar_arrive_expect_tx(&full[s], (uint32_t)I8_BLOCK + cbytes);
                 tc::bulk_load(st, pa + (size_t)p * I8_BLOCK, (uint32_t)I8_BLOCK, &full[s]);
@@ -752,7 +763,12 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
             int Q, mb, chunk;
             tr_item(a, item, Q, mb, chunk);
             const int m = mb * MM + rr;
-            const bool valid = m < a.nbf;
+            bool valid = m < a.nbf;
+            // the row's weight and its nocc_p elements of X (read back after the first run)
+            if (valid && (!BCHK((size_t)Q * a.nbf_p + m < a.lim_sA, a.err, BC_TR_SA, (size_t)Q * a.nbf_p + m, a.lim_sA) ||
+                          !BRANGE((size_t)m * a.kdim_b + (size_t)(Q - a.q0) * a.nocc_p, a.nocc_p, a.lim_X, a.err,
+                                  BC_TR_X)))
+                valid = false;
             const float sa = valid ? a.sA[(size_t)Q * a.nbf_p + m] : 0.f;
             float2* xrow = a.Xdf + (valid ? (size_t)m * a.kdim_b + (size_t)(Q - a.q0) * a.nocc_p : 0);
             float rmax = 0.f;
@@ -809,7 +825,9 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                 __syncwarp();
                 if ((threadIdx.x % 32) == 0) tc::mbar_arrive(&tempty[buf]);
             }
-            if (ok && valid && rmax > 0.f)
+            if (ok && valid && rmax > 0.f &&
+                BCHK((size_t)m * a.ngroups + (Q - a.q0) / a.G < a.lim_xmax, a.err, BC_TR_XMAX,
+                     (size_t)m * a.ngroups + (Q - a.q0) / a.G, a.lim_xmax))
                 atomicMax(&a.xmax[(size_t)m * a.ngroups + (Q - a.q0) / a.G], __float_as_uint(rmax));
         }
     }
@@ -832,14 +850,20 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
 __global__ void __launch_bounds__(256) oz_split_X_kernel(const float2* __restrict__ Xdf, const unsigned* __restrict__ xmax,
                                                          int nbf, int nbf_p, int ngroups, int G, int nq, int nocc_p,
                                                          size_t kdim_b, size_t nkbt, float* __restrict__ Sx,
-                                                         __nv_bfloat16* __restrict__ Xd) {
+                                                         __nv_bfloat16* __restrict__ Xd, size_t lim_X, size_t lim_Xd,
+                                                         size_t lim_Sx, int* __restrict__ err) {
     const int mb = blockIdx.x, g = blockIdx.y;
     __shared__ int Es[MM];
     if (threadIdx.x < MM) {
         const int m = mb * MM + threadIdx.x;
-        const int E = m < nbf ? exp_of_max_f(xmax[(size_t)m * ngroups + g]) : E_EMPTY;
+        int E = m < nbf ? exp_of_max_f(xmax[(size_t)m * ngroups + g]) : E_EMPTY;
+        // the row's X elements of this group
+        const size_t kb0 = (size_t)g * G * nocc_p / MK, kb1 = (size_t)min(nq, (g + 1) * G) * nocc_p / MK;
+        if (E != E_EMPTY && !BRANGE((size_t)m * kdim_b + kb0 * MK, (kb1 - kb0) * MK, lim_X, err, BC_SX_READ))
+            E = E_EMPTY;
         Es[threadIdx.x] = E;
-        Sx[(size_t)g * nbf_p + m] = scale_of(E);
+        if (BCHK((size_t)g * nbf_p + m < lim_Sx, err, BC_SX_SX, (size_t)g * nbf_p + m, lim_Sx))
+            Sx[(size_t)g * nbf_p + m] = scale_of(E);
     }
     __syncthreads();
     const int kb0 = g * G * nocc_p / MK;
@@ -870,6 +894,7 @@ __global__ void __launch_bounds__(256) oz_split_X_kernel(const float2* __restric
         }
         __nv_bfloat16* base = Xd + ((size_t)mb * nkbt + kb) * NSL * (MM * MK);
         const uint32_t off = tc::swz_offset((uint32_t)r, (uint32_t)c) / 2;
+        if (!BRANGE(((size_t)mb * nkbt + kb) * NSL * (MM * MK), (size_t)NSL * MM * MK, lim_Xd, err, BC_SX_WRITE)) continue;
 #pragma unroll
         for (int s = 0; s < NSL; ++s)
             *reinterpret_cast<uint4*>(base + (size_t)s * (MM * MK) + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
@@ -893,6 +918,8 @@ struct CtArgs {
     int M, N, accumulate;
     int stages, n_items;
     int* err;
+    // extents in elements (checked in the bounds-checked build); lim_out covers part or out
+    size_t lim_Xd, lim_Yd, lim_Sx, lim_Sy, lim_out;
 };
 
 // Stage per k block: [NS A slices, 128 rows | NS B slices, 64 rows], both read by the MMAs
@@ -964,6 +991,14 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                 const int kb0 = ct_kb0(a, g), kb1 = ct_kb1(a, g);
                 for (int kb = kb0; kb < kb1; ++kb, ++kg) {
                     if (kg >= a.stages && !tc::mbar_wait(&empty[s], ph ^ 1u, abort_flag, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    if (!BRANGE(((size_t)tb.x * a.nkbt + kb) * NS * blk, (size_t)NS * blk, a.lim_Xd, a.err, BC_CT_A) ||
+                        !BRANGE((size_t)(tb.y / 2) * a.nkbt * NS * blk + (size_t)(tb.y % 2) * (CT_N * MK) +
+                                    ((size_t)kb * NS + NS - 1) * blk,
+                                CT_N * MK, a.lim_Yd, a.err, BC_CT_B)) {
+                        *abort_flag = 1;
                         ok = false;
                         break;
                     }
@@ -1051,6 +1086,12 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                     ok = false;
                     break;
                 }
+                if (!BCHK((size_t)g * a.lds_x + m < a.lim_Sx, a.err, BC_CT_S, (size_t)g * a.lds_x + m, a.lim_Sx) ||
+                    !BRANGE((size_t)g * a.lds_y + n0, HC, a.lim_Sy, a.err, BC_CT_S)) {
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
                 tc::tc_fence_after();
                 const float rs = a.Sx[(size_t)g * a.lds_x + m];
                 const float* cs = a.Sy + (size_t)g * a.lds_y + n0;
@@ -1082,9 +1123,9 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
             if (!ok) break;
             if constexpr (DIRECT) {
                 // general product: the rows and columns that exist, (+)= into out
-                if (m < a.M) {
+                const int nv = min(HC, a.N - n0);
+                if (m < a.M && (nv <= 0 || BRANGE((size_t)m * a.ldo + n0, nv, a.lim_out, a.err, BC_CT_OUT))) {
                     double* dst = a.out + (size_t)m * a.ldo + n0;
-                    const int nv = min(HC, a.N - n0);
 #pragma unroll
                     for (int c = 0; c < HC; ++c)
                         if (c < nv) {
@@ -1094,6 +1135,7 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
                 }
             } else {
                 double* dst = a.part + (((size_t)(item / a.ntiles) * a.ntiles + tile) * MM + r) * CT_N + half * HC;
+                if (!BRANGE((size_t)(dst - a.part), HC, a.lim_out, a.err, BC_CT_OUT)) continue;
 #pragma unroll
                 for (int c = 0; c < HC; c += 2)
                     *reinterpret_cast<double2*>(dst + c) =
@@ -1114,7 +1156,8 @@ __global__ void __launch_bounds__(CT_THREADS, 1) oz_contract_kernel(const CtArgs
 
 // K[m][n] (and its mirror), m >= n, = [K +] sum over splits (fixed order) of the partial tiles.
 __global__ void oz_reduce_kernel(const double* __restrict__ part, int nsplit, int ntiles, int nbf,
-                                 const int* __restrict__ tob, int ncb, double* __restrict__ K, int accumulate) {
+                                 const int* __restrict__ tob, int ncb, double* __restrict__ K, int accumulate,
+                                 size_t lim_part, int* __restrict__ err) {
     const size_t n_lower = (size_t)nbf * (nbf + 1) / 2;
     const size_t tstride = (size_t)ntiles * MM * CT_N;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n_lower; p += (size_t)gridDim.x * blockDim.x) {
@@ -1124,6 +1167,9 @@ __global__ void oz_reduce_kernel(const double* __restrict__ part, int nsplit, in
         const size_t n = p - m * (m + 1) / 2;
         const int t = tob[(m / MM) * ncb + n / CT_N];
         const size_t off = ((size_t)t * MM + (m % MM)) * CT_N + (n % CT_N);
+        if (!BCHK(t >= 0, err, BC_RED, t, ntiles) ||
+            !BRANGE((size_t)(nsplit - 1) * tstride + off, 1, lim_part, err, BC_RED))
+            continue;
         double s = 0.0;
         for (int k = 0; k < nsplit; ++k) s += part[(size_t)k * tstride + off];
         if (accumulate) s += K[m * nbf + n];
@@ -1656,6 +1702,11 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
             ta.nbuf = (2 * TR_NACC * N <= TR_ACOL0) ? 2 : 1;
             ta.n_items = nq * nmb * nchunk;
             ta.err = o->err;
+            ta.lim_Bd = (size_t)naux * ob->nnz * I8_BLOCK;
+            ta.lim_Cd = side ? o->Cr_cap : o->C_cap;
+            ta.lim_X = (size_t)nbf * o->X_cap;
+            ta.lim_xmax = o->xm_cap;
+            ta.lim_sA = (size_t)naux * nbf_p;
             const int ev = 2 * (nsides * batch + side);
             cudaEventRecord(o->tr_ev[ev], s);
             oz_transform_kernel<<<(unsigned)std::min(ta.n_items, o->num_sms), TR_THREADS, SMEM_BUDGET, s>>>(ta);
@@ -1664,7 +1715,8 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
             if (ev_transform_done && q0 + qb >= naux && side == nsides - 1) cudaEventRecord(ev_transform_done, s);
             oz_split_X_kernel<<<dim3((unsigned)nmb, (unsigned)ngroups), 256, 0, s>>>(
                 o->Xdf, o->xmax, nbf, nbf_p, ngroups, G, nq, nocc_p, kdim_b, nkbt, side ? o->Sx_r : o->Sx,
-                side ? o->Xd_r : o->Xd);
+                side ? o->Xd_r : o->Xd, (size_t)nbf * o->X_cap, (size_t)nbf_p * (side ? o->Xr_cap : o->X_cap) * NSL,
+                side ? o->sxr_cap : o->sx_cap, o->err);
         }
         if (nonsym) {
             // K (+)= X_left X_right^T over every tile, written straight into K (nbf x nbf)
@@ -1690,6 +1742,11 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
             ca.stages = ct_stages;
             ca.n_items = o->ntiles_all;
             ca.err = o->err;
+            ca.lim_Xd = (size_t)nbf_p * o->X_cap * NSL;
+            ca.lim_Yd = (size_t)nbf_p * o->Xr_cap * NSL;
+            ca.lim_Sx = o->sx_cap;
+            ca.lim_Sy = o->sxr_cap;
+            ca.lim_out = (size_t)nbf * nbf;
             ct_nonsym_kernel()<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
             continue;
         }
@@ -1721,10 +1778,14 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         ca.stages = ct_stages;
         ca.n_items = o->ntiles * nsplit;
         ca.err = o->err;
+        ca.lim_Xd = ca.lim_Yd = (size_t)nbf_p * o->X_cap * NSL;
+        ca.lim_Sx = ca.lim_Sy = o->sx_cap;
+        ca.lim_out = o->part_cap;
         ct_sym_kernel()<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
         const size_t nl = (size_t)nbf * (nbf + 1) / 2;
         const int blocks = (int)std::min<size_t>((nl + 255) / 256, (size_t)o->num_sms * 16);
-        oz_reduce_kernel<<<blocks, 256, 0, s>>>(o->part, nsplit, o->ntiles, nbf, o->d_tob, o->ncb, K, batch > 0 ? 1 : 0);
+        oz_reduce_kernel<<<blocks, 256, 0, s>>>(o->part, nsplit, o->ntiles, nbf, o->d_tob, o->ncb, K, batch > 0 ? 1 : 0,
+                                                 o->part_cap, o->err);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -1865,6 +1926,11 @@ int oz_gemm(OzState* o, const double* A, size_t lda, const double* B, size_t ldb
         ca.stages = ct_stages;
         ca.n_items = ca.ntiles;
         ca.err = o->err;
+        ca.lim_Xd = (size_t)M_pad * K_pad * GM_NS;
+        ca.lim_Yd = (size_t)nc * K_pad * GM_NS;
+        ca.lim_Sx = (size_t)ngroups * M_pad;
+        ca.lim_Sy = (size_t)ngroups * nc;
+        ca.lim_out = (size_t)(M - 1) * ldc + (size_t)(N - c0);
         ct_gemm_kernel()<<<(unsigned)std::min(ca.n_items, o->num_sms), CT_THREADS, SMEM_BUDGET, s>>>(ca);
     }
     cudaError_t e = cudaGetLastError();

@@ -24,6 +24,16 @@ def test_gdfjk_exports_every_declared_symbol(jk_built):
     assert sorted(_jkabi.SIGNATURES) == names
 
 
+def test_bounds_checked_build_exports_every_declared_symbol(jk_built):
+    """-DGDFJK_BOUNDS_CHECK compiles (the checks are live in this build) into its own library
+    with the same interface."""
+    path = _native.build_jk(bounds_check=True)
+    assert path == _native.JK_BCHK_SO and path != _native.JK_SO
+    lib = ctypes.CDLL(path)
+    for n in _declared("gdfjk.h", "gdfjk"):
+        assert hasattr(lib, n), n
+
+
 def test_gdfints_exports_every_declared_symbol(ints_built):
     lib = ctypes.CDLL(_native.INTS_SO)
     for n in _declared("gdfints.h", "gdfints"):
