@@ -4,9 +4,10 @@
  * The engine replaces the JK half of psi4's in-core DF path: MemDFJK::compute_JK
  * (psi4/src/psi4/libfock/MemDFJK.cc:97-111) -> DFHelper::build_JK / compute_JK /
  * compute_J_symm / compute_K (psi4/src/psi4/lib3index/dfhelper.cc:3015-3377).  The
- * metric-contracted 3-index tensor B[Q][mn] = sum_P J^-1/2_QP (P|mn) is built on the
- * host (as DFHelper::prepare_AO_core does, dfhelper.cc:514-588), uploaded to HBM once,
- * and every Fock build then runs on the GPU.
+ * metric-contracted 3-index tensor B[Q][mn] = sum_P J^-1/2_QP (P|mn) is built as
+ * DFHelper::prepare_AO_core builds it (dfhelper.cc:514-588), either on the host and uploaded
+ * to HBM once, or on the device from its own raw integrals and metric contraction, and
+ * every Fock build then runs on the GPU.
  *
  * Conventions: row-major FP64 host/device matrices; every call returns an int status
  * (GDFJK_OK = 0, negative on error) and gdfjk_last_error(h) gives the message (h may be
@@ -93,6 +94,35 @@ int gdfjk_upload_B_device(gdfjk_t h, const double* B_qtri_device);
  * that ends at naux has been uploaded.  Neither call keeps the pointer. */
 int gdfjk_upload_B_block(gdfjk_t h, const double* B_qtri_rows, int q0, int nq);
 int gdfjk_upload_B_device_block(gdfjk_t h, const double* B_qtri_rows_device, int q0, int nq);
+
+/* ---- The raw integrals on the device (DFHelper::prepare_AO_core's integral step,
+ * dfhelper.cc:514-588: compute_sparse_pQq_blocking_p_symm, :1284-1347, with libint2's
+ * 3-index ERIs; the metric of FittingMetric::form_fitting_metric, fittingmetric.cc:72).
+ * McMurchie-Davidson per shell triplet on the FP64 pipes; primary shells up to f, fitting
+ * shells up to g; both bases pure (psi4's default for the cc-pVXZ families) or both
+ * Cartesian.  Component order and normalisation are those of the host provider (gdfints). */
+typedef struct gdfjk_basis_s* gdfjk_basis_t;
+
+/* A basis set copied to CUDA device `device`: nshell shells with angular momentum l[s],
+ * nprim[s] primitives exps/coefs[prim_offset[s] ...] (raw contraction coefficients, normalised
+ * here as psi4 normalises them), centres xyz[3*s..] in bohr; puream != 0: solid harmonics. */
+int gdfjk_basis_create(int device, int nshell, const int* l, const int* nprim, const int* prim_offset,
+                       const double* exps, const double* coefs, const double* xyz, int puream, gdfjk_basis_t* out);
+void gdfjk_basis_destroy(gdfjk_basis_t b);
+int gdfjk_basis_nbf(gdfjk_basis_t b);
+
+/* (P|mn) for fitting functions p0 <= P < p1 and the primary shell pairs M >= N with
+ * shell_mask[M*nshell + N] != 0 (host, nullable = every pair; DFHelper's Schwarz shell mask,
+ * dfhelper.cc:336-366), written into the device array out, row P - p0 at out + (P - p0)*ldo:
+ * column m(m+1)/2 + n (m >= n) when col_map is NULL (ldo >= nbf(nbf+1)/2), else column
+ * col_map[m(m+1)/2 + n] (a device array of nbf(nbf+1)/2 entries; < 0 = not stored).  Entries
+ * of unlisted pairs are not written (zero the array first).  Runs on `stream` (a
+ * cudaStream_t, NULL = the default stream) and returns when the integrals are complete. */
+int gdfjk_three_index_device(gdfjk_basis_t aux, gdfjk_basis_t prim, const unsigned char* shell_mask, int p0, int p1,
+                             const int64_t* col_map, int64_t ldo, double* out, void* stream);
+
+/* The Coulomb metric (P|Q), rows p0 <= P < p1 at out + (P - p0)*ldo, all naux columns. */
+int gdfjk_metric_device(gdfjk_basis_t aux, int p0, int p1, int64_t ldo, double* out, void* stream);
 
 /* The metric contraction B = J^-1/2 (P|mn) on the tensor cores, to FP64 accuracy (the
  * emulated-FP64 digit products of GDFJK_EMULATED): replaces the naux x naux DGEMM of

@@ -31,7 +31,9 @@ JK_SO = os.path.join(LIB, "libgdfjk.so")
 JK_BCHK_SO = os.path.join(LIB, "libgdfjk_bchk.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-JK_SOURCES = ["gdfjk_host.cu", "j_kernels.cu", "k_fp64.cu", "k_mixed.cu", "k_oz.cu", "backward.cu", "noalloc.cu"]
+# ints3c_lc*.cu (the integral class kernels) come first: they take the longest to compile
+JK_SOURCES = ["ints3c_lc2.cu", "ints3c_lc3.cu", "ints3c_lc1.cu", "ints3c_lc4.cu", "ints3c_lc0.cu", "k_oz.cu", "k_mixed.cu",
+              "gdfjk_host.cu", "j_kernels.cu", "k_fp64.cu", "backward.cu", "noalloc.cu", "ints3c.cu"]
 
 _lock = threading.Lock()
 
@@ -89,7 +91,7 @@ def build_jk(force: bool = False, extra_flags=None, bounds_check: bool = False) 
         _run([nvcc] + flags + ["-c", src, "-o", obj])
         return obj
 
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with ThreadPoolExecutor(max_workers=min(max(4, os.cpu_count() or 4), len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     _run([nvcc] + ARCH + ["-shared", "-o", out + ".tmp"] + objs)
     os.replace(out + ".tmp", out)

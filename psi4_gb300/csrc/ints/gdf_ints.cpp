@@ -21,6 +21,7 @@
 // recursion.  Solid harmonics from the closed form in MEST eq. 6.4.47-6.4.50.
 
 #include "gdfints.h"
+#include "gto_tables.h"
 
 #include <algorithm>
 #include <cmath>
@@ -109,29 +110,16 @@ const TuvTable& tuvs() {
 // ---------------------------------------------------------------- Boys function
 struct Boys {
     static constexpr int NMAX = RDIM + 2;
-    static constexpr int KT = 7;
-    static constexpr double TMAX = 40.0;
-    static constexpr double H = 0.025;
+    static constexpr int KT = gto::BOYS_KT;
+    static constexpr double TMAX = gto::BOYS_TMAX;
+    static constexpr double H = gto::BOYS_H;
     int ngrid;
     int stride;
     std::vector<double> tab;
     Boys() {
-        ngrid = static_cast<int>(TMAX / H) + 2;
+        ngrid = gto::boys_ngrid();
         stride = NMAX + KT + 1;
-        tab.assign(static_cast<size_t>(ngrid) * stride, 0.0);
-        for (int g = 0; g < ngrid; ++g) {
-            long double T = static_cast<long double>(g) * H;
-            for (int n = 0; n < stride; ++n) {
-                long double term = 1.0L / (2 * n + 1);
-                long double sum = term;
-                for (int k = 1; k < 2000; ++k) {
-                    term *= 2.0L * T / (2 * n + 2 * k + 1);
-                    sum += term;
-                    if (term < 1e-22L * sum) break;
-                }
-                tab[static_cast<size_t>(g) * stride + n] = static_cast<double>(std::exp(-T) * sum);
-            }
-        }
+        tab = gto::boys_grid(ngrid, stride, H);
     }
     // F[0..n]
     void eval(int n, double T, double* F) const {
@@ -166,42 +154,7 @@ const Boys& boys() {
 struct PureTable {
     std::vector<double> c[MAXL + 1];
     PureTable() {
-        const auto& ct = carts();
-        for (int l = 0; l <= MAXL; ++l) {
-            int nc = ncart(l);
-            c[l].assign((2 * l + 1) * nc, 0.0);
-            for (int r = 0; r < 2 * l + 1; ++r) {
-                int m = (r == 0) ? 0 : ((r % 2 == 1) ? (r + 1) / 2 : -(r / 2));
-                int am = std::abs(m);
-                double* row = &c[l][r * nc];
-                int vstart2 = (m >= 0) ? 0 : 1;  // 2*v_m
-                for (int t = 0; t <= (l - am) / 2; ++t)
-                    for (int u = 0; u <= t; ++u)
-                        for (int v2 = vstart2; v2 <= am; v2 += 2) {
-                            double sgn = (((t + (v2 - vstart2) / 2) % 2) == 0) ? 1.0 : -1.0;
-                            double coef = sgn * std::pow(0.25, t) * binom(l, t) * binom(l - t, am + t) *
-                                          binom(t, u) * binom(am, v2);
-                            int px = 2 * t + am - 2 * u - v2;
-                            int py = 2 * u + v2;
-                            int pz = l - 2 * t - am;
-                            for (int k = 0; k < nc; ++k)
-                                if (ct.comp[l][k][0] == px && ct.comp[l][k][1] == py && ct.comp[l][k][2] == pz)
-                                    row[k] += coef;
-                        }
-                // normalise: components share the radial part and the x^l normalisation
-                double nrm = 0.0;
-                for (int a = 0; a < nc; ++a)
-                    for (int b = 0; b < nc; ++b) {
-                        int sx = ct.comp[l][a][0] + ct.comp[l][b][0];
-                        int sy = ct.comp[l][a][1] + ct.comp[l][b][1];
-                        int sz = ct.comp[l][a][2] + ct.comp[l][b][2];
-                        if ((sx | sy | sz) & 1) continue;
-                        nrm += row[a] * row[b] * dfact(sx - 1) * dfact(sy - 1) * dfact(sz - 1) / dfact(2 * l - 1);
-                    }
-                double s = 1.0 / std::sqrt(nrm);
-                for (int k = 0; k < nc; ++k) row[k] *= s;
-            }
-        }
+        for (int l = 0; l <= MAXL; ++l) c[l] = gto::pure_matrix(l);
     }
 };
 const PureTable& pures() {
@@ -558,20 +511,7 @@ int gdfints_basis_create(int nshell, const int* l, const int* nprim, const int* 
             for (int d = 0; d < 3; ++d) sh.O[d] = xyz[3 * s + d];
             sh.a.assign(exps + prim_offset[s], exps + prim_offset[s] + sh.nprim);
             sh.c.assign(coefs + prim_offset[s], coefs + prim_offset[s] + sh.nprim);
-            // primitive normalisation of the x^l component
-            for (int k = 0; k < sh.nprim; ++k) {
-                double a = sh.a[k];
-                sh.c[k] *= std::pow(2.0 * a / M_PI, 0.75) * std::pow(4.0 * a, 0.5 * sh.l) / std::sqrt(dfact(2 * sh.l - 1));
-            }
-            // contracted normalisation
-            double nrm = 0.0;
-            for (int i = 0; i < sh.nprim; ++i)
-                for (int j = 0; j < sh.nprim; ++j) {
-                    double g = sh.a[i] + sh.a[j];
-                    nrm += sh.c[i] * sh.c[j] * std::pow(M_PI / g, 1.5) * dfact(2 * sh.l - 1) / std::pow(2.0 * g, sh.l);
-                }
-            double sc = 1.0 / std::sqrt(nrm);
-            for (auto& c : sh.c) c *= sc;
+            gto::normalise_shell(sh.l, sh.nprim, sh.a.data(), sh.c.data());
             b->sh.push_back(std::move(sh));
         }
         b->nbf = off;

@@ -1,0 +1,8 @@
+// ints3c_lc2.cu — the 3-index integral class kernels with fitting shells of angular momentum 2.
+#include "ints3c.cuh"
+
+namespace gdfjk {
+namespace ints {
+Eri3Kernel pick_lc2(int la, int lb) { return pick_pair<2>(la, lb); }
+}  // namespace ints
+}  // namespace gdfjk

@@ -1,18 +1,22 @@
 """B = J^-1/2 (P|mn) built on the device for large systems (the caller's initialisation).
 
 This is psi4's ``DFHelper::prepare_AO_core`` (psi4/src/psi4/lib3index/dfhelper.cc:514-588)
-arranged for one GB300: the raw 3-index integrals (P|mn) come from the host integral
-provider in blocks of aux rows (``compute_sparse_pQq_blocking_p_symm``, dfhelper.cc:1284-1347)
-and are copied into one device array; the metric contraction (``contract_metric_AO_core_symm``,
+arranged for one GB300: the raw 3-index integrals (P|mn) of the Schwarz-significant shell
+pairs (``compute_sparse_pQq_blocking_p_symm``, dfhelper.cc:1284-1347) and the metric (P|Q)
+(``FittingMetric::form_fitting_metric``, fittingmetric.cc:72) are computed by the engine's
+integral kernels straight into device arrays (``gdfjk_three_index_device``,
+``gdfjk_metric_device``; ``device_integrals=False`` takes them from the host provider
+instead, in blocks of aux rows); the metric contraction (``contract_metric_AO_core_symm``,
 dfhelper.cc:1653-1678) runs on the tensor cores to FP64 accuracy
 (``gdfjk_metric_contract_device``); B is then relaid into the engine's tiles
-(``gdfjk_upload_B_device``).  Screening and the metric power are the host restatements of
-``dfhelper.py`` (prepare_sparsity, Matrix::power).
+(``gdfjk_upload_B_device``).  Screening (the Schwarz diagonal) and the metric power are the
+host restatements of ``dfhelper.py`` (prepare_sparsity, Matrix::power).
 
 torch supplies the device arrays (plumbing); every computation on them is the engine's.
 """
 from __future__ import annotations
 
+import ctypes
 import time
 from dataclasses import dataclass, field
 
@@ -21,8 +25,71 @@ import numpy as np
 from .basis import BasisSet
 from .dfhelper import DEFAULT_CONDITION, DEFAULT_CUTOFF, Sparsity, metric_power, prepare_sparsity
 from .ints import Integrals
-from .jk import DFJKEngine
+from .jk import DFJKEngine, GdfjkError
 from .molecule import Molecule
+
+
+class DeviceBasis:
+    """A basis set copied to a CUDA device for the engine's integral kernels
+    (gdfjk_basis_create): shells, primitives and normalised contraction coefficients."""
+
+    def __init__(self, bs: BasisSet, device: int = 0):
+        from . import _native
+
+        self.L = _native.jk_lib()
+        self.bs = bs
+        self.device = device
+        self._keep = [np.ascontiguousarray(x) for x in (bs.l.astype(np.int32), bs.nprim.astype(np.int32),
+                                                        bs.prim_offset.astype(np.int32), bs.exps, bs.coefs,
+                                                        bs.centers.reshape(-1))]
+        l, npr, off, ex, cf, xyz = self._keep
+        h = ctypes.c_void_p()
+        rc = self.L.gdfjk_basis_create(int(device), bs.nshell, _p(l), _p(npr), _p(off), _p(ex), _p(cf), _p(xyz),
+                                       int(bs.puream), ctypes.byref(h))
+        if rc != 0:
+            raise GdfjkError(rc, self.L.gdfjk_last_error(None).decode())
+        self.h = h
+        self.nbf = self.L.gdfjk_basis_nbf(h)
+        assert self.nbf == bs.nbf
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gdfjk_basis_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def three_index_device(aux: DeviceBasis, prim: DeviceBasis, out_ptr: int, ldo: int, shell_mask=None, p0: int = 0,
+                       p1: int | None = None, col_map_ptr: int | None = None, stream: int | None = None):
+    """(P|mn), p0 <= P < p1, for the shell pairs M >= N of shell_mask (None: all) into the
+    device array at out_ptr (row P - p0 at out_ptr + 8 (P - p0) ldo; column m(m+1)/2+n, or
+    col_map[m(m+1)/2+n] when col_map_ptr is given).  Unlisted pairs are not written."""
+    p1 = aux.nbf if p1 is None else p1
+    mask = None if shell_mask is None else np.ascontiguousarray(shell_mask, dtype=np.uint8)
+    rc = aux.L.gdfjk_three_index_device(aux.h, prim.h, None if mask is None else _p(mask), int(p0), int(p1),
+                                        None if col_map_ptr is None else ctypes.c_void_p(col_map_ptr), int(ldo),
+                                        ctypes.c_void_p(out_ptr), None if not stream else ctypes.c_void_p(stream))
+    if rc != 0:
+        raise GdfjkError(rc, aux.L.gdfjk_last_error(None).decode())
+
+
+def metric_device(aux: DeviceBasis, out_ptr: int, ldo: int, p0: int = 0, p1: int | None = None,
+                  stream: int | None = None):
+    """The Coulomb metric (P|Q), rows p0 <= P < p1, into the device array at out_ptr."""
+    p1 = aux.nbf if p1 is None else p1
+    rc = aux.L.gdfjk_metric_device(aux.h, int(p0), int(p1), int(ldo), ctypes.c_void_p(out_ptr),
+                                   None if not stream else ctypes.c_void_p(stream))
+    if rc != 0:
+        raise GdfjkError(rc, aux.L.gdfjk_last_error(None).decode())
 
 
 @dataclass
@@ -38,38 +105,97 @@ class DeviceDF:
     rows: np.ndarray | None = None  # the first `keep_rows` rows of B (packed triangle), host copy
 
 
+def metric_power_device(Md, power: float, condition: float):
+    """Matrix::power (matrix.cc:2370-2415) of a device matrix, with the host restatement's
+    rule (dfhelper.metric_power): eigendecompose (the library's FP64 symmetric eigensolver),
+    drop |lambda| < condition * max|lambda| for negative powers, rebuild V diag(lambda^p) V^T."""
+    import torch
+
+    w, V = torch.linalg.eigh(Md)
+    max_a = torch.maximum(w[-1].abs(), w[0].abs())
+    a = torch.where(w > 0, w.clamp(min=torch.finfo(w.dtype).tiny) ** power, torch.zeros_like(w))
+    if power < 0.0:
+        a = torch.where(w.abs() < condition * max_a, torch.zeros_like(a), a)
+    a = torch.where(torch.isfinite(a), a, torch.zeros_like(a))
+    return (V * a) @ V.T
+
+
+def _metric_and_power(ints, aux_dev, naux, condition, dev, timings, power_on="host"):
+    """(P|Q) (on the device when aux_dev is given) and J^-1/2 (Matrix::power on the host, or
+    on the device with power_on="device"); returns (M, J^-1/2 on the host, J^-1/2 on the device)."""
+    import torch
+
+    tm = time.perf_counter()
+    if aux_dev is not None:
+        Md = torch.empty((naux, naux), dtype=torch.float64, device=dev)
+        metric_device(aux_dev, Md.data_ptr(), naux)
+    else:
+        Md = torch.from_numpy(ints.metric()).to(dev)
+    M = Md.cpu().numpy()
+    tp = time.perf_counter()
+    if power_on == "device":
+        Jm = metric_power_device(Md, -0.5, condition)
+        Jm_host = Jm.cpu().numpy()
+        timings.update({"metric_s": tp - tm, "metric_power_device_s": time.perf_counter() - tp})
+    else:
+        Jm_host = metric_power(M, -0.5, condition)
+        Jm = torch.from_numpy(Jm_host).to(dev).contiguous()
+        timings.update({"metric_s": tp - tm, "metric_power_host_s": time.perf_counter() - tp})
+    del Md
+    return M, Jm_host, Jm
+
+
 def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int = 0, cutoff: float = DEFAULT_CUTOFF,
                    condition: float = DEFAULT_CONDITION, ints: Integrals | None = None, block: int = 128,
-                   keep_rows: int = 0, check_columns: int = 0) -> DeviceDF:
+                   keep_rows: int = 0, check_columns: int = 0, device_integrals: bool = True,
+                   metric_power_on: str = "host") -> DeviceDF:
     """Build B on the device and upload it into a new engine.  `keep_rows` > 0 also returns a
     host copy of B's first rows (for checks against a CPU restatement); `check_columns` > 0
     compares that many columns of the tensor-core metric contraction with the FP64 library
-    GEMM and records the largest difference in ``timings``."""
+    GEMM and records the largest difference in ``timings``.  device_integrals: (P|mn) and
+    (P|Q) from the engine's integral kernels (else from the host provider); metric_power_on:
+    "host" (psi4's Matrix::power restated) or "device" (the same rule on the library's FP64
+    eigensolver)."""
     import torch
 
     dev = torch.device("cuda", device)
     t0 = time.perf_counter()
     ints = ints or Integrals(mol, primary, aux)
     nbf, naux = primary.nbf, aux.nbf
+    timings = {}
+    ts = time.perf_counter()
     fun_max, shell_max = ints.schwarz()
     sp = prepare_sparsity(fun_max, shell_max, cutoff, naux)
-    M = ints.metric()
-    Jm_host = metric_power(M, -0.5, condition)
-    Jm = torch.from_numpy(Jm_host).to(dev).contiguous()
+    timings["schwarz_and_sparsity_host_s"] = time.perf_counter() - ts
+    pb_dev = ab_dev = None
+    if device_integrals:
+        pb_dev, ab_dev = DeviceBasis(primary, device), DeviceBasis(aux, device)
+    M, Jm_host, Jm = _metric_and_power(ints, ab_dev, naux, condition, dev, timings, metric_power_on)
     r, c = np.tril_indices(nbf)
     keep = torch.from_numpy(sp.pair_mask[r, c].astype(np.float64)).to(dev)
     npair = keep.numel()
-    P = torch.empty((naux, npair), dtype=torch.float64, device=dev)
     t_ints = t_copy = 0.0
-    for p0 in range(0, naux, block):
-        p1 = min(naux, p0 + block)
+    if device_integrals:
         ta = time.perf_counter()
-        A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
-        t_ints += time.perf_counter() - ta
-        tb = time.perf_counter()
-        P[p0:p1] = torch.from_numpy(A).to(dev) * keep  # screened pairs are absent from psi4's tensor
+        P = torch.zeros((naux, npair), dtype=torch.float64, device=dev)
+        three_index_device(ab_dev, pb_dev, P.data_ptr(), npair, shell_mask=sp.shell_mask)
+        P *= keep  # screened pairs are absent from psi4's tensor
         torch.cuda.synchronize(dev)
-        t_copy += time.perf_counter() - tb
+        timings["three_index_device_s"] = time.perf_counter() - ta
+        pb_dev.close()
+        ab_dev.close()
+    else:
+        P = torch.empty((naux, npair), dtype=torch.float64, device=dev)
+        for p0 in range(0, naux, block):
+            p1 = min(naux, p0 + block)
+            ta = time.perf_counter()
+            A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
+            t_ints += time.perf_counter() - ta
+            tb = time.perf_counter()
+            P[p0:p1] = torch.from_numpy(A).to(dev) * keep  # screened pairs are absent from psi4's tensor
+            torch.cuda.synchronize(dev)
+            t_copy += time.perf_counter() - tb
+        timings.update({"three_index_host_s": t_ints, "three_index_copy_s": t_copy})
     del keep
     eng = DFJKEngine(nbf, naux, sp.pair_mask, device=device)
     B = torch.empty((naux, npair), dtype=torch.float64, device=dev)
@@ -77,7 +203,7 @@ def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int 
     tg = time.perf_counter()
     eng.metric_contract(Jm.data_ptr(), P.data_ptr(), npair, B.data_ptr())
     t_gemm = time.perf_counter() - tg
-    timings = {"three_index_host_s": t_ints, "three_index_copy_s": t_copy, "metric_contraction_device_s": t_gemm}
+    timings["metric_contraction_device_s"] = t_gemm
     if check_columns > 0:
         nc = min(npair, check_columns)
         (Jm @ P[:, :1024]).sum().item()  # the library GEMM's first-call set-up stays out of its time
@@ -101,44 +227,62 @@ def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int 
 
 def build_device_B_screened(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int = 0,
                             cutoff: float = DEFAULT_CUTOFF, condition: float = DEFAULT_CONDITION,
-                            ints: Integrals | None = None, block: int = 128, upload_rows: int = 256) -> DeviceDF:
+                            ints: Integrals | None = None, block: int = 128, upload_rows: int = 256,
+                            device_integrals: bool = True, metric_power_on: str = "host") -> DeviceDF:
     """build_device_B for systems whose dense packed triangle would not fit the device (the
     C100H202 workload: 271 GB dense, 10 % of the pairs significant): (P|mn) is held on the device
     over the Schwarz-significant pairs only (m >= n, DFHelper's sparse tensor), contracted with
     J^-1/2 there, and B is expanded back to packed-triangle rows a block of aux functions at a
     time for the engine's block upload (gdfjk_upload_B_device_block), which keeps only the
-    stored tiles."""
+    stored tiles.  device_integrals as in build_device_B (the kernels write the significant
+    pairs' columns through a column map)."""
     import torch
 
     dev = torch.device("cuda", device)
     t0 = time.perf_counter()
     ints = ints or Integrals(mol, primary, aux)
     nbf, naux = primary.nbf, aux.nbf
+    timings = {}
+    ts = time.perf_counter()
     fun_max, shell_max = ints.schwarz()
     sp = prepare_sparsity(fun_max, shell_max, cutoff, naux)
+    timings["schwarz_and_sparsity_host_s"] = time.perf_counter() - ts
     r, c = np.tril_indices(nbf)
     sig = np.flatnonzero(sp.pair_mask[r, c])  # packed-triangle columns of the significant pairs
     npair, nsig = r.size, sig.size
-    M = ints.metric()
-    tm = time.perf_counter()
-    Jm_host = metric_power(M, -0.5, condition)
-    t_metric = time.perf_counter() - tm
+    pb_dev = ab_dev = None
+    if device_integrals:
+        pb_dev, ab_dev = DeviceBasis(primary, device), DeviceBasis(aux, device)
+    M, Jm_host, Jm = _metric_and_power(ints, ab_dev, naux, condition, dev, timings, metric_power_on)
     sig_d = torch.from_numpy(sig).to(dev)
-    P = torch.empty((naux, nsig), dtype=torch.float64, device=dev)
     t_ints = t_copy = 0.0
-    for p0 in range(0, naux, block):
-        p1 = min(naux, p0 + block)
+    if device_integrals:
         ta = time.perf_counter()
-        A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
-        As = np.ascontiguousarray(A[:, sig])
-        del A
-        t_ints += time.perf_counter() - ta
-        tb = time.perf_counter()
-        P[p0:p1] = torch.from_numpy(As).to(dev)
-        t_copy += time.perf_counter() - tb
-    torch.cuda.synchronize(dev)
+        col_map = np.full(npair, -1, dtype=np.int64)
+        col_map[sig] = np.arange(nsig, dtype=np.int64)
+        col_d = torch.from_numpy(col_map).to(dev)
+        P = torch.zeros((naux, nsig), dtype=torch.float64, device=dev)
+        three_index_device(ab_dev, pb_dev, P.data_ptr(), nsig, shell_mask=sp.shell_mask, col_map_ptr=col_d.data_ptr())
+        torch.cuda.synchronize(dev)
+        del col_d
+        timings["three_index_device_s"] = time.perf_counter() - ta
+        pb_dev.close()
+        ab_dev.close()
+    else:
+        P = torch.empty((naux, nsig), dtype=torch.float64, device=dev)
+        for p0 in range(0, naux, block):
+            p1 = min(naux, p0 + block)
+            ta = time.perf_counter()
+            A = ints.three_index(shell_mask=sp.shell_mask, p0=p0, p1=p1)
+            As = np.ascontiguousarray(A[:, sig])
+            del A
+            t_ints += time.perf_counter() - ta
+            tb = time.perf_counter()
+            P[p0:p1] = torch.from_numpy(As).to(dev)
+            t_copy += time.perf_counter() - tb
+        torch.cuda.synchronize(dev)
+        timings.update({"three_index_host_s": t_ints, "three_index_copy_s": t_copy})
     eng = DFJKEngine(nbf, naux, sp.pair_mask, device=device)
-    Jm = torch.from_numpy(Jm_host).to(dev)
     Bs = torch.empty_like(P)
     tg = time.perf_counter()
     eng.metric_contract(Jm.data_ptr(), P.data_ptr(), nsig, Bs.data_ptr())
@@ -155,9 +299,8 @@ def build_device_B_screened(mol: Molecule, primary: BasisSet, aux: BasisSet, dev
     del rows, Bs
     torch.cuda.empty_cache()
     t_up = time.perf_counter() - tu
-    timings = {"three_index_host_s": t_ints, "three_index_copy_s": t_copy, "metric_power_host_s": t_metric,
-               "metric_contraction_device_s": t_gemm, "expand_and_upload_s": t_up, "significant_pairs": int(nsig),
-               "pairs": int(npair), "total_s": time.perf_counter() - t0}
+    timings.update({"metric_contraction_device_s": t_gemm, "expand_and_upload_s": t_up, "significant_pairs": int(nsig),
+                    "pairs": int(npair), "total_s": time.perf_counter() - t0})
     return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, None)
 
 
