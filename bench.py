@@ -433,6 +433,14 @@ def run_gpu(args):
         except Exception as ex:
             out["metric_contraction"] = {"unavailable": str(ex)[:300]}
         torch.cuda.empty_cache()
+    if rank == 0 and args.ints:
+        out["integrals"] = {}
+        for cfg in [c for c in args.ints.split(",") if c]:
+            try:
+                out["integrals"][cfg] = measure_integrals(cfg, dev)
+            except Exception as ex:
+                out["integrals"][cfg] = {"unavailable": str(ex)[:300]}
+            torch.cuda.empty_cache()
     if rank == 0 and args.host_b:
         out["host_b"] = {}
         for cfg in [c for c in args.host_b.split(",") if c]:
@@ -967,6 +975,78 @@ def measure_scf(cfg):
             "time_to_converge_speedup": t64 / tmx}
 
 
+def measure_integrals(cfg, dev, host_rows=64):
+    """The raw integrals of B's initialisation on the device (gdfjk_three_index_device over the
+    Schwarz-significant shell pairs, gdfjk_metric_device) for a real molecule of the workload,
+    against the host provider on the first `host_rows` fitting functions (seconds scaled by the
+    rows; the host's cost per row is even across the aux basis up to shell-size effects, the
+    comparison shows the agreement).  C5 writes the significant pairs' columns through a column
+    map (the screened build's layout); the others the dense packed triangle."""
+    import torch
+
+    from psi4_gb300.basis import BasisSet
+    from psi4_gb300.device_init import DeviceBasis, metric_device, three_index_device
+    from psi4_gb300.dfhelper import DEFAULT_CUTOFF, prepare_sparsity
+    from psi4_gb300.ints import Integrals
+    from psi4_gb300.molecule import linear_alkane, water_cluster
+
+    gen, basis, desc = CONFIGS[cfg]
+    screened = "alkane" in gen
+    mol = linear_alkane(gen["alkane"], seed=0) if screened else water_cluster(*gen["lattice"], seed=0)
+    pb = BasisSet.build(mol, basis)
+    ab = BasisSet.fitting_for(mol, pb)
+    ints = Integrals(mol, pb, ab)
+    nbf, naux = pb.nbf, ab.nbf
+    t0 = time.perf_counter()
+    fun_max, shell_max = ints.schwarz()
+    sp = prepare_sparsity(fun_max, shell_max, DEFAULT_CUTOFF, naux)
+    t_schwarz = time.perf_counter() - t0
+    pd, ad = DeviceBasis(pb, dev.index or 0), DeviceBasis(ab, dev.index or 0)
+    r, c = np.tril_indices(nbf)
+    npair = r.size
+    col_d = None
+    if screened:
+        sig = np.flatnonzero(sp.pair_mask[r, c])
+        col_map = np.full(npair, -1, dtype=np.int64)
+        col_map[sig] = np.arange(sig.size, dtype=np.int64)
+        col_d = torch.from_numpy(col_map).to(dev)
+        ncols, cols = sig.size, sig
+    else:
+        ncols, cols = npair, None
+    P = torch.zeros((naux, ncols), dtype=torch.float64, device=dev)
+    kw = dict(shell_mask=sp.shell_mask, col_map_ptr=None if col_d is None else col_d.data_ptr())
+    three_index_device(ad, pd, P.data_ptr(), ncols, p1=min(naux, 32), **kw)  # module load, tables
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    three_index_device(ad, pd, P.data_ptr(), ncols, **kw)
+    torch.cuda.synchronize(dev)
+    t_dev = time.perf_counter() - t0
+    Md = torch.empty((naux, naux), dtype=torch.float64, device=dev)
+    t0 = time.perf_counter()
+    metric_device(ad, Md.data_ptr(), naux)
+    torch.cuda.synchronize(dev)
+    t_metric = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref = ints.three_index(shell_mask=sp.shell_mask, p0=0, p1=host_rows)
+    t_host = time.perf_counter() - t0
+    if cols is not None:
+        ref = ref[:, cols]
+    d = float(np.abs(P[:host_rows].cpu().numpy() - ref).max())
+    t0 = time.perf_counter()
+    Mh = ints.metric()
+    t_metric_host = time.perf_counter() - t0
+    dm = float(np.abs(Md.cpu().numpy() - Mh).max())
+    nsig_sh = int(np.tril(sp.shell_mask).sum())
+    return {"workload": f"{desc} (real molecule)", "nbf": nbf, "naux": naux, "primary_shells": int(pb.nshell),
+            "fitting_shells": int(ab.nshell), "significant_shell_pairs": nsig_sh, "columns": int(ncols),
+            "three_index_device_s": t_dev, "metric_device_s": t_metric, "schwarz_and_sparsity_host_s": t_schwarz,
+            "three_index_host_s_scaled": t_host * naux / host_rows,
+            "three_index_host_sample": f"first {host_rows} fitting functions in {t_host:.3f} s, scaled by naux/{host_rows}",
+            "metric_host_s": t_metric_host, "speedup_three_index": t_host * naux / host_rows / t_dev,
+            "max_abs_diff_vs_host_sample": d, "max_abs_diff_metric_vs_host": dm,
+            "shell_triplets_per_s": nsig_sh * ab.nshell / t_dev}
+
+
 def measure_gradient(cfg, dev):
     """The differentiation form at a configuration: SCF to convergence in the emulated FP64
     form on real integrals, then the analytic nuclear gradient — the engine's backward (dE/dB
@@ -1075,6 +1155,7 @@ def main():
     ap.add_argument("--grad-config", default="c4", help="analytic-gradient leg ('' for none)")
     ap.add_argument("--extra", default="c1,c4,c3,c5", help="comma-separated extra configurations (synthetic B), '' for none")
     ap.add_argument("--metric", default="c2", help="configuration of the metric-contraction leg, '' for none")
+    ap.add_argument("--ints", default="c2", help="configurations of the device-integral leg, '' for none")
     ap.add_argument("--host-b", default="c4,c2",
                     help="configurations measured with B in pinned host memory (GDFJK_B_HOST), '' for none")
     args = ap.parse_args()

@@ -120,10 +120,20 @@ def metric_power_device(Md, power: float, condition: float):
     return (V * a) @ V.T
 
 
-def _metric_and_power(ints, aux_dev, naux, condition, dev, timings, power_on="host"):
+# "auto": the device eigensolver from this many fitting functions on (measured on GB300 against
+# the 16 host cores: n = 4448 host 1.45 s / device 0.74 s plus ~3.5 s of the library's set-up
+# on first use; n = 7424 6.9 / 2.9 s; n = 11646 27.6 / 10.3 s)
+METRIC_POWER_DEVICE_FROM = 6000
+
+
+def _metric_and_power(ints, aux_dev, naux, condition, dev, timings, power_on="auto"):
     """(P|Q) (on the device when aux_dev is given) and J^-1/2 (Matrix::power on the host, or
-    on the device with power_on="device"); returns (M, J^-1/2 on the host, J^-1/2 on the device)."""
+    on the device with power_on="device"; "auto" picks by size); returns (M, J^-1/2 on the
+    host, J^-1/2 on the device)."""
     import torch
+
+    if power_on == "auto":
+        power_on = "device" if naux >= METRIC_POWER_DEVICE_FROM else "host"
 
     tm = time.perf_counter()
     if aux_dev is not None:
@@ -148,14 +158,14 @@ def _metric_and_power(ints, aux_dev, naux, condition, dev, timings, power_on="ho
 def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int = 0, cutoff: float = DEFAULT_CUTOFF,
                    condition: float = DEFAULT_CONDITION, ints: Integrals | None = None, block: int = 128,
                    keep_rows: int = 0, check_columns: int = 0, device_integrals: bool = True,
-                   metric_power_on: str = "host") -> DeviceDF:
+                   metric_power_on: str = "auto") -> DeviceDF:
     """Build B on the device and upload it into a new engine.  `keep_rows` > 0 also returns a
     host copy of B's first rows (for checks against a CPU restatement); `check_columns` > 0
     compares that many columns of the tensor-core metric contraction with the FP64 library
     GEMM and records the largest difference in ``timings``.  device_integrals: (P|mn) and
     (P|Q) from the engine's integral kernels (else from the host provider); metric_power_on:
-    "host" (psi4's Matrix::power restated) or "device" (the same rule on the library's FP64
-    eigensolver)."""
+    "host" (psi4's Matrix::power restated), "device" (the same rule on the library's FP64
+    eigensolver) or "auto" (the device from METRIC_POWER_DEVICE_FROM fitting functions)."""
     import torch
 
     dev = torch.device("cuda", device)
@@ -228,7 +238,7 @@ def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int 
 def build_device_B_screened(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int = 0,
                             cutoff: float = DEFAULT_CUTOFF, condition: float = DEFAULT_CONDITION,
                             ints: Integrals | None = None, block: int = 128, upload_rows: int = 256,
-                            device_integrals: bool = True, metric_power_on: str = "host") -> DeviceDF:
+                            device_integrals: bool = True, metric_power_on: str = "auto") -> DeviceDF:
     """build_device_B for systems whose dense packed triangle would not fit the device (the
     C100H202 workload: 271 GB dense, 10 % of the pairs significant): (P|mn) is held on the device
     over the Schwarz-significant pairs only (m >= n, DFHelper's sparse tensor), contracted with
