@@ -105,9 +105,11 @@ typedef struct gdfjk_basis_s* gdfjk_basis_t;
 
 /* A basis set copied to CUDA device `device`: nshell shells with angular momentum l[s],
  * nprim[s] primitives exps/coefs[prim_offset[s] ...] (raw contraction coefficients, normalised
- * here as psi4 normalises them), centres xyz[3*s..] in bohr; puream != 0: solid harmonics. */
+ * here as psi4 normalises them), centres xyz[3*s..] in bohr, atom[s] the atom of the shell's
+ * centre (nullable; needed by the gradient entries); puream != 0: solid harmonics. */
 int gdfjk_basis_create(int device, int nshell, const int* l, const int* nprim, const int* prim_offset,
-                       const double* exps, const double* coefs, const double* xyz, int puream, gdfjk_basis_t* out);
+                       const double* exps, const double* coefs, const double* xyz, const int* atom, int puream,
+                       gdfjk_basis_t* out);
 void gdfjk_basis_destroy(gdfjk_basis_t b);
 int gdfjk_basis_nbf(gdfjk_basis_t b);
 
@@ -123,6 +125,21 @@ int gdfjk_three_index_device(gdfjk_basis_t aux, gdfjk_basis_t prim, const unsign
 
 /* The Coulomb metric (P|Q), rows p0 <= P < p1 at out + (P - p0)*ldo, all naux columns. */
 int gdfjk_metric_device(gdfjk_basis_t aux, int p0, int p1, int64_t ldo, double* out, void* stream);
+
+/* The gradient's derivative-integral contractions on the device (DFJKGrad::build_Amn_x_terms,
+ * jk_grad.cc:868-1245; MintsHelper::metric_grad, mintshelper.cc:2388), added into the device
+ * array grad[natom][3]:
+ *   three_index_grad: sum over P and the listed shell pairs of G3[P][col(m,n)] d(P|mn)/dx,
+ *       G3 a device array laid out as gdfjk_three_index_device's output (all naux rows,
+ *       leading dimension ldg, packed-triangle columns or col_map), off-diagonal mn entries
+ *       carrying the weight of both (mn) and (nm);
+ *   metric_grad: sum over P, Q of G2[P][Q] d(P|Q)/dx, G2 symmetric, naux x naux, ldg >= naux.
+ * Both bases need atom indices.  Summed with atomics (the order of the additions is not
+ * fixed; results agree to rounding).  Return when complete. */
+int gdfjk_three_index_grad_device(gdfjk_basis_t aux, gdfjk_basis_t prim, const unsigned char* shell_mask,
+                                  const double* G3, const int64_t* col_map, int64_t ldg, int natom, double* grad,
+                                  void* stream);
+int gdfjk_metric_grad_device(gdfjk_basis_t aux, const double* G2, int64_t ldg, int natom, double* grad, void* stream);
 
 /* The metric contraction B = J^-1/2 (P|mn) on the tensor cores, to FP64 accuracy (the
  * emulated-FP64 digit products of GDFJK_EMULATED): replaces the naux x naux DGEMM of

@@ -16,11 +16,13 @@ SIGNATURES = {
     "gdfjk_trim": (I, [P]),
     "gdfjk_metric_contract_device": (I, [P, P, P, I, ctypes.c_int64, P, ctypes.c_int64, I]),
     "gdfjk_gemm_device": (I, [P, I, I, I, I, P, ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64, I]),
-    "gdfjk_basis_create": (I, [I, I, P, P, P, P, P, P, I, ctypes.POINTER(P)]),
+    "gdfjk_basis_create": (I, [I, I, P, P, P, P, P, P, P, I, ctypes.POINTER(P)]),
     "gdfjk_basis_destroy": (None, [P]),
     "gdfjk_basis_nbf": (I, [P]),
     "gdfjk_three_index_device": (I, [P, P, P, I, I, P, ctypes.c_int64, P, P]),
     "gdfjk_metric_device": (I, [P, I, I, ctypes.c_int64, P, P]),
+    "gdfjk_three_index_grad_device": (I, [P, P, P, P, P, ctypes.c_int64, I, P, P]),
+    "gdfjk_metric_grad_device": (I, [P, P, ctypes.c_int64, I, P, P]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_wK": (I, [P, P, P, P, I, I, I, P]),

@@ -36,9 +36,9 @@
 struct gdfjk_basis_s {
     int device = 0;
     int nshell = 0, nbf = 0, puream = 1, maxl = 0;
-    std::vector<int> l, nprim, poff, foff;
+    std::vector<int> l, nprim, poff, foff, atom;
     std::vector<double> xyz;
-    int *d_l = nullptr, *d_nprim = nullptr, *d_poff = nullptr, *d_foff = nullptr;
+    int *d_l = nullptr, *d_nprim = nullptr, *d_poff = nullptr, *d_foff = nullptr, *d_atom = nullptr;
     double *d_xyz = nullptr, *d_exps = nullptr, *d_coefs = nullptr;
 };
 
@@ -46,6 +46,7 @@ namespace gdfjk {
 namespace ints {
 
 int ppw(int la, int lb) { return 5 + 3 * (la + 1) * (lb + 1) * (la + lb + 1); }
+int ppw_grad(int la, int lb) { return 7 + 3 * (la + 2) * (lb + 2) * (la + lb + 3); }
 
 
 Eri3Kernel pick(int la, int lb, int lc) {
@@ -99,7 +100,7 @@ int device_tables(int device, const double** boys_out, const double** pure_out, 
 }
 
 Shells shells_of(const gdfjk_basis_s* b) {
-    return Shells{b->d_l, b->d_nprim, b->d_poff, b->d_foff, b->d_xyz, b->d_exps, b->d_coefs};
+    return Shells{b->d_atom, b->d_l, b->d_nprim, b->d_poff, b->d_foff, b->d_xyz, b->d_exps, b->d_coefs};
 }
 
 // device copies of the class lists of one call, released on return
@@ -185,6 +186,83 @@ int run_classes(const gdfjk_basis_s* ab, const gdfjk_basis_s* cs, const std::vec
     return GDFJK_OK;
 }
 
+Eri3GradKernel pick_grad(int la, int lb, int lc) {
+    switch (lc) {
+        case 0: return pick_grad_lc0(la, lb);
+        case 1: return pick_grad_lc1(la, lb);
+        case 2: return pick_grad_lc2(la, lb);
+        case 3: return pick_grad_lc3(la, lb);
+        case 4: return pick_grad_lc4(la, lb);
+        default: return nullptr;
+    }
+}
+
+// The derivative classes, as run_classes; the gradient is accumulated with atomics.
+int run_grad_classes(const gdfjk_basis_s* ab, const gdfjk_basis_s* cs, const std::vector<int2>* pair_cls,
+                     int npair_cls, const std::vector<int>* fit_cls, Eri3GradArgs base, cudaStream_t stream,
+                     std::string& err) {
+    const double *boys = nullptr, *pure = nullptr;
+    int rc = device_tables(ab->device, &boys, &pure, err);
+    if (rc) return rc;
+    base.boys = boys;
+    base.pure = pure;
+    base.ab = shells_of(ab);
+    base.cs = shells_of(cs);
+    ListBuffers lists;
+    for (int pc = 0; pc < npair_cls; ++pc) {
+        const std::vector<int2>& pl = pair_cls[pc];
+        if (pl.empty()) continue;
+        const int la = ab->l[pl[0].x], lb = pl[0].y < 0 ? 0 : ab->l[pl[0].y];
+        int max_pp = 1;
+        for (const int2& q : pl) max_pp = std::max(max_pp, ab->nprim[q.x] * (q.y < 0 ? 1 : ab->nprim[q.y]));
+        const size_t smem = (size_t)max_pp * ppw_grad(la, lb) * sizeof(double);
+        int2* d_pairs = nullptr;
+        if ((rc = lists.upload(pl, &d_pairs, err))) return rc;
+        for (int lc = 0; lc <= MAXL_FIT; ++lc) {
+            const std::vector<int>& fl = fit_cls[lc];
+            if (fl.empty()) continue;
+            Eri3GradKernel k = pick_grad(la, lb, lc);
+            if (!k) {
+                err = "integral derivatives: no kernel for the angular momenta (" + std::to_string(la) + " " +
+                      std::to_string(lb) + " | " + std::to_string(lc) + ")";
+                return GDFJK_ERR_ARG;
+            }
+            if (smem > 40 * 1024) {
+                if (smem > 200 * 1024) {
+                    err = "integral derivatives: too many primitive products in one shell pair";
+                    return GDFJK_ERR_ARG;
+                }
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            }
+            int* d_fits = nullptr;
+            if ((rc = lists.upload(fl, &d_fits, err))) return rc;
+            Eri3GradArgs args = base;
+            args.pairs = d_pairs;
+            args.fits = d_fits;
+            args.nfit = (int)fl.size();
+            const dim3 grid((unsigned)pl.size(), (unsigned)((fl.size() + ERI_THREADS - 1) / ERI_THREADS));
+            k<<<grid, ERI_THREADS, smem, stream>>>(args);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) {
+                err = std::string("integral derivatives: launch failed: ") + cudaGetErrorString(e);
+                return GDFJK_ERR_CUDA;
+            }
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        err = std::string("integral derivatives: ") + cudaGetErrorString(e);
+        return GDFJK_ERR_CUDA;
+    }
+    return GDFJK_OK;
+}
+
+bool atoms_valid(const gdfjk_basis_s* b, int natom) {
+    for (int a : b->atom)
+        if (a < 0 || a >= natom) return false;
+    return true;
+}
+
 }  // namespace ints
 }  // namespace gdfjk
 
@@ -193,7 +271,7 @@ using namespace gdfjk;
 extern "C" {
 
 int gdfjk_basis_create(int device, int nshell, const int* l, const int* nprim, const int* prim_offset, const double* exps,
-                       const double* coefs, const double* xyz, int puream, gdfjk_basis_t* out) {
+                       const double* coefs, const double* xyz, const int* atom, int puream, gdfjk_basis_t* out) {
     if (!out || nshell <= 0 || !l || !nprim || !prim_offset || !exps || !coefs || !xyz)
         return report_error(GDFJK_ERR_ARG, "basis_create: null argument or no shells");
     auto* b = new gdfjk_basis_s();
@@ -214,6 +292,7 @@ int gdfjk_basis_create(int device, int nshell, const int* l, const int* nprim, c
     for (int s = 0; s < nshell; ++s) {
         gto::normalise_shell(l[s], nprim[s], exps + prim_offset[s], c.data() + prim_offset[s]);
         b->l.push_back(l[s]);
+        b->atom.push_back(atom ? atom[s] : -1);
         b->nprim.push_back(nprim[s]);
         b->poff.push_back(prim_offset[s]);
         b->foff.push_back(off);
@@ -230,6 +309,7 @@ int gdfjk_basis_create(int device, int nshell, const int* l, const int* nprim, c
         return cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
     };
     const bool ok = up((void**)&b->d_l, b->l.data(), nshell * sizeof(int)) &&
+                    up((void**)&b->d_atom, b->atom.data(), nshell * sizeof(int)) &&
                     up((void**)&b->d_nprim, b->nprim.data(), nshell * sizeof(int)) &&
                     up((void**)&b->d_poff, b->poff.data(), nshell * sizeof(int)) &&
                     up((void**)&b->d_foff, b->foff.data(), nshell * sizeof(int)) &&
@@ -248,7 +328,7 @@ int gdfjk_basis_create(int device, int nshell, const int* l, const int* nprim, c
 
 void gdfjk_basis_destroy(gdfjk_basis_t b) {
     if (!b) return;
-    void* ps[] = {b->d_l, b->d_nprim, b->d_poff, b->d_foff, b->d_xyz, b->d_exps, b->d_coefs};
+    void* ps[] = {b->d_l, b->d_atom, b->d_nprim, b->d_poff, b->d_foff, b->d_xyz, b->d_exps, b->d_coefs};
     for (void* p : ps)
         if (p) cudaFree(p);
     delete b;
@@ -329,6 +409,75 @@ int gdfjk_metric_device(gdfjk_basis_t aux, int p0, int p1, int64_t ldo, double* 
     base.metric = 1;
     std::string err;
     const int rc = ints::run_classes(aux, aux, pairs, ints::MAXL_FIT + 1, fits, base, (cudaStream_t)stream, err);
+    cudaSetDevice(cur);
+    return rc ? report_error(rc, err) : GDFJK_OK;
+}
+
+int gdfjk_three_index_grad_device(gdfjk_basis_t aux, gdfjk_basis_t prim, const unsigned char* shell_mask,
+                                  const double* G3, const int64_t* col_map, int64_t ldg, int natom, double* grad,
+                                  void* stream) {
+    if (!aux || !prim || !G3 || !grad) return report_error(GDFJK_ERR_ARG, "three_index_grad_device: null argument");
+    if (aux->device != prim->device)
+        return report_error(GDFJK_ERR_ARG, "three_index_grad_device: bases on different devices");
+    const long long npair = (long long)prim->nbf * (prim->nbf + 1) / 2;
+    if (ldg < (col_map ? 1 : npair)) return report_error(GDFJK_ERR_ARG, "three_index_grad_device: leading dimension too small");
+    if (prim->maxl > ints::MAXL_PAIR)
+        return report_error(GDFJK_ERR_ARG, "three_index_grad_device: primary shells above f are not supported");
+    if (aux->puream != prim->puream)
+        return report_error(GDFJK_ERR_ARG, "three_index_grad_device: the two bases must agree on pure/Cartesian");
+    if (natom <= 0 || !ints::atoms_valid(prim, natom) || !ints::atoms_valid(aux, natom))
+        return report_error(GDFJK_ERR_ARG, "three_index_grad_device: the bases need atom indices below natom");
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(prim->device);
+    const int nsp = prim->nshell;
+    std::vector<int2> pairs[(ints::MAXL_PAIR + 1) * (ints::MAXL_PAIR + 1)];
+    for (int M = 0; M < nsp; ++M)
+        for (int N = 0; N <= M; ++N) {
+            if (shell_mask && !shell_mask[(size_t)M * nsp + N]) continue;
+            const int lm = prim->l[M], ln = prim->l[N];
+            const int2 pr = lm >= ln ? make_int2(M, N) : make_int2(N, M);
+            pairs[std::max(lm, ln) * (ints::MAXL_PAIR + 1) + std::min(lm, ln)].push_back(pr);
+        }
+    std::vector<int> fits[ints::MAXL_FIT + 1];
+    for (int P = 0; P < aux->nshell; ++P) fits[aux->l[P]].push_back(P);
+    ints::Eri3GradArgs base{};
+    base.pure_ab = prim->puream;
+    base.pure_c = aux->puream;
+    base.G = G3;
+    base.ldg = ldg;
+    base.col_map = reinterpret_cast<const long long*>(col_map);
+    base.grad = grad;
+    base.metric = 0;
+    std::string err;
+    const int rc = ints::run_grad_classes(prim, aux, pairs, (int)(sizeof(pairs) / sizeof(pairs[0])), fits, base,
+                                          (cudaStream_t)stream, err);
+    cudaSetDevice(cur);
+    return rc ? report_error(rc, err) : GDFJK_OK;
+}
+
+int gdfjk_metric_grad_device(gdfjk_basis_t aux, const double* G2, int64_t ldg, int natom, double* grad, void* stream) {
+    if (!aux || !G2 || !grad) return report_error(GDFJK_ERR_ARG, "metric_grad_device: null argument");
+    if (ldg < aux->nbf) return report_error(GDFJK_ERR_ARG, "metric_grad_device: leading dimension below naux");
+    if (natom <= 0 || !ints::atoms_valid(aux, natom))
+        return report_error(GDFJK_ERR_ARG, "metric_grad_device: the basis needs atom indices below natom");
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(aux->device);
+    std::vector<int2> pairs[ints::MAXL_FIT + 1];
+    for (int Q = 0; Q < aux->nshell; ++Q) pairs[aux->l[Q]].push_back(make_int2(Q, -1));
+    std::vector<int> fits[ints::MAXL_FIT + 1];
+    for (int P = 0; P < aux->nshell; ++P) fits[aux->l[P]].push_back(P);
+    ints::Eri3GradArgs base{};
+    base.pure_ab = aux->puream;
+    base.pure_c = aux->puream;
+    base.G = G2;
+    base.ldg = ldg;
+    base.col_map = nullptr;
+    base.grad = grad;
+    base.metric = 1;
+    std::string err;
+    const int rc = ints::run_grad_classes(aux, aux, pairs, ints::MAXL_FIT + 1, fits, base, (cudaStream_t)stream, err);
     cudaSetDevice(cur);
     return rc ? report_error(rc, err) : GDFJK_OK;
 }

@@ -12,7 +12,7 @@ namespace ints {
 
 constexpr int MAXL_PAIR = 3;  // primary shells: up to f
 constexpr int MAXL_FIT = 4;   // fitting shells: up to g (also the metric's row shells)
-constexpr int BOYS_NMAX = 2 * MAXL_PAIR + MAXL_FIT;
+constexpr int BOYS_NMAX = 2 * MAXL_PAIR + MAXL_FIT + 1;  // + 1: first derivatives
 constexpr int BOYS_STRIDE = BOYS_NMAX + gto::BOYS_KT + 1;
 constexpr int ERI_THREADS = 64;
 
@@ -32,6 +32,7 @@ __host__ __device__ constexpr int pure_off(int l) { return l == 0 ? 0 : l == 1 ?
 constexpr int PURE_TABLE = 245;  // sum over l <= 4 of (2l+1) ncart(l)
 
 struct Shells {
+    const int* atom;  // atom of each shell (the gradients' centres)
     const int* l;
     const int* nprim;
     const int* poff;
@@ -464,11 +465,248 @@ __global__ void __launch_bounds__(ERI_THREADS) eri3c_kernel(const Eri3Args a) {
     }
 }
 
+// ---------------------------------------------------------------- first derivatives
+// The gradient's contraction of the 3-index density with derivative integrals (psi4's
+// DFJKGrad::build_Amn_x_terms, psi4/src/psi4/scfgrad/jk_grad.cc:868-1245, and the metric's
+// MintsHelper::metric_grad, psi4/src/psi4/libmints/mintshelper.cc:2388):
+//   grad[atom(A)] += sum G[P][mn] d(P|mn)/dA, grad[atom(B)] += ... d/dB,
+//   grad[atom(C)] -= both (translational invariance), C the fitting shell.
+// Derivatives of the Gaussians (d/dA_x x_A^i e^{-a x_A^2} = 2a x_A^(i+1) e^.. - i x_A^(i-1) e^..)
+// fold into the pair's Hermite coefficients, so the Hermite sums run one order higher.  The
+// density block is taken from solid harmonics to Cartesian components once per triplet and
+// contracted on the fly: no derivative integral is stored.
+struct Eri3GradArgs {
+    Shells ab, cs;
+    const int2* pairs;
+    const int* fits;
+    int nfit;
+    int pure_ab, pure_c;
+    const double* G;           // density rows: row P at G + P * ldg, columns as Eri3Args' out
+    long long ldg;
+    const long long* col_map;  // nullable
+    double* grad;              // [natom][3], accumulated
+    const double* boys;
+    const double* pure;
+    int metric;                // 1: G[P][Q] against (P|Q), the pair being (Q, unit)
+};
+
+// adjoint of to_pure: pure components in the first 2l+1 slots of the index -> all ncart slots
+template <int L, int OUTER, int SO, int SI, int INNER>
+__device__ __forceinline__ void from_pure(const double* __restrict__ c_pure, double* blk) {
+    constexpr int NC = ncart(L), NP = 2 * L + 1;
+    if constexpr (L > 0) {
+#pragma unroll 1
+        for (int o = 0; o < OUTER; ++o)
+#pragma unroll 1
+            for (int i = 0; i < INNER; ++i) {
+                double tmp[NC];
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    double s = 0.0;
+#pragma unroll
+                    for (int r = 0; r < NP; ++r) s = fma(__ldg(c_pure + pure_off(L) + r * NC + k), blk[o * SO + r * SI + i], s);
+                    tmp[k] = s;
+                }
+#pragma unroll
+                for (int k = 0; k < NC; ++k) blk[o * SO + k * SI + i] = tmp[k];
+            }
+    }
+}
+
+template <int LA, int LB, int LC>
+__global__ void __launch_bounds__(ERI_THREADS) eri3c_grad_kernel(const Eri3GradArgs a) {
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC);
+    constexpr int LAB = LA + LB, LW = LAB + 1, L = LW + LC;
+    constexpr int NTW = ntuv(LW), NTL = ntuv(L);
+    constexpr int TE = LAB + 3;                  // t range of E with i <= LA+1, j <= LB+1
+    constexpr int ED = (LA + 2) * (LB + 2) * TE;
+    constexpr int PPW = 7 + 3 * ED;              // p, P, coefficient product, a, b, E tables
+    extern __shared__ double shp[];
+    __shared__ double red[6][ERI_THREADS];
+    const int2 pr = a.pairs[blockIdx.x];
+    const int sa = pr.x, sb = pr.y;
+    const bool unit_b = sb < 0;
+    const double* Ac = a.ab.xyz + 3 * sa;
+    const double* Bc = unit_b ? Ac : a.ab.xyz + 3 * sb;
+    const int npa = a.ab.nprim[sa], npb = unit_b ? 1 : a.ab.nprim[sb];
+    const int npp = npa * npb;
+    for (int k = threadIdx.x; k < npp; k += blockDim.x) {
+        const int ia = k / npb, ib = k % npb;
+        const double ea = a.ab.exps[a.ab.poff[sa] + ia];
+        const double eb = unit_b ? 0.0 : a.ab.exps[a.ab.poff[sb] + ib];
+        const double p = ea + eb;
+        double* w = shp + (size_t)k * PPW;
+        w[0] = p;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) w[1 + d] = (ea * Ac[d] + eb * Bc[d]) / p;
+        w[4] = a.ab.coefs[a.ab.poff[sa] + ia] * (unit_b ? 1.0 : a.ab.coefs[a.ab.poff[sb] + ib]);
+        w[5] = ea;
+        w[6] = eb;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) hermite_1d<LA + 1, LB + 1>(ea, eb, Ac[d], Bc[d], w + 7 + d * ED);
+    }
+    __syncthreads();
+    const int atomA = a.ab.atom[sa], atomB = unit_b ? atomA : a.ab.atom[sb];
+    const int ci = blockIdx.y * blockDim.x + threadIdx.x;
+    double gA[3] = {0.0, 0.0, 0.0}, gB[3] = {0.0, 0.0, 0.0};
+    int atomC = -1;
+    if (ci < a.nfit) {
+        const int sc = a.fits[ci];
+        atomC = a.cs.atom[sc];
+        if (!(atomA == atomB && atomB == atomC)) {
+            // the density block in solid harmonics, then in Cartesian components
+            double g[NA * NB * NC];
+#pragma unroll 1
+            for (int k = 0; k < NA * NB * NC; ++k) g[k] = 0.0;
+            const int na = a.pure_ab ? 2 * LA + 1 : NA, nb = unit_b ? 1 : (a.pure_ab ? 2 * LB + 1 : NB);
+            const int nc = a.pure_c ? 2 * LC + 1 : NC;
+            const int fa = a.ab.foff[sa], fb = unit_b ? 0 : a.ab.foff[sb], fc = a.cs.foff[sc];
+#pragma unroll 1
+            for (int q = 0; q < nc; ++q) {
+                const double* row = a.G + (size_t)(fc + q) * a.ldg;
+#pragma unroll 1
+                for (int ka = 0; ka < na; ++ka) {
+                    const long long m = fa + ka;
+#pragma unroll 1
+                    for (int kb = 0; kb < nb; ++kb) {
+                        double v;
+                        if (a.metric) {
+                            v = row[m];
+                        } else {
+                            const long long n = fb + kb;
+                            if (sa == sb && m < n) continue;  // diagonal shell pair: the lower triangle
+                            long long col = m >= n ? m * (m + 1) / 2 + n : n * (n + 1) / 2 + m;
+                            if (a.col_map) col = a.col_map[col];
+                            v = col < 0 ? 0.0 : row[col];
+                        }
+                        g[(ka * NB + kb) * NC + q] = v;
+                    }
+                }
+            }
+            if (a.pure_c) from_pure<LC, NA * NB, NC, 1, 1>(a.pure, g);
+            if (a.pure_ab) {
+                from_pure<LB, NA, NB * NC, NC, NC>(a.pure, g);
+                from_pure<LA, 1, 0, NB * NC, NB * NC>(a.pure, g);
+            }
+            const double* Cc = a.cs.xyz + 3 * sc;
+            const int npc = a.cs.nprim[sc], pc0 = a.cs.poff[sc];
+            constexpr double TWO_PI_52 = 34.986836655249725;
+            constexpr double SGN = (LC & 1) ? -1.0 : 1.0;
+#pragma unroll 1
+            for (int k = 0; k < npp; ++k) {
+                const double* w = shp + (size_t)k * PPW;
+                const double p = w[0], ea2 = 2.0 * w[5], eb2 = 2.0 * w[6];
+                const double* E[3] = {w + 7, w + 7 + ED, w + 7 + 2 * ED};
+#pragma unroll 1
+                for (int kc = 0; kc < npc; ++kc) {
+                    const double c = a.cs.exps[pc0 + kc];
+                    const double pc = p + c, alpha = p * c / pc;
+                    const double X = w[1] - Cc[0], Y = w[2] - Cc[1], Z = w[3] - Cc[2];
+                    double F[L + 1];
+                    boys<L>(a.boys, alpha * (X * X + Y * Y + Z * Z), F);
+                    double R[NTL];
+                    hermite_r<L, false>(alpha, X, Y, Z, F, R);
+                    const double pref = SGN * TWO_PI_52 / (p * c * sqrt(pc)) * w[4] * a.cs.coefs[pc0 + kc];
+                    double Ec[(LC + 1) * (LC + 1)];
+#pragma unroll
+                    for (int q = 0; q < (LC + 1) * (LC + 1); ++q) Ec[q] = 0.0;
+                    Ec[0] = 1.0;
+                    const double o2c = 0.5 / c;
+#pragma unroll
+                    for (int i = 0; i < LC; ++i)
+#pragma unroll
+                        for (int t = 0; t <= LC; ++t)
+                            if (t <= i + 1) {
+                                double v = 0.0;
+                                if (t > 0) v += o2c * Ec[i * (LC + 1) + t - 1];
+                                if (t + 1 <= i) v += (t + 1) * Ec[i * (LC + 1) + t + 1];
+                                Ec[(i + 1) * (LC + 1) + t] = v;
+                            }
+#pragma unroll 1
+                    for (int kq = 0; kq < NC; ++kq) {
+                        double W[NTW];
+                        ket_sum_loop<LW, LC, L>(Ec, R, cart_x(LC, kq), cart_y(kq), cart_z(kq), W);
+#pragma unroll 1
+                        for (int ka = 0; ka < NA; ++ka)
+#pragma unroll 1
+                            for (int kb = 0; kb < NB; ++kb) {
+                                const double gv = g[(ka * NB + kb) * NC + kq];
+                                if (gv == 0.0) continue;
+                                const int ii[3] = {cart_x(LA, ka), cart_y(ka), cart_z(ka)};
+                                const int jj[3] = {cart_x(LB, kb), cart_y(kb), cart_z(kb)};
+                                const double* e0[3];  // E(i, j) rows of the three dimensions
+#pragma unroll
+                                for (int d = 0; d < 3; ++d) e0[d] = E[d] + (ii[d] * (LB + 2) + jj[d]) * TE;
+                                const double f = pref * gv;
+#pragma unroll
+                                for (int d = 0; d < 3; ++d) {
+                                    // d/dA_d: 2a E(i+1, j) - i E(i-1, j) in dimension d
+                                    double dA[TE], dB[TE];
+                                    const double* up = E[d] + ((ii[d] + 1) * (LB + 2) + jj[d]) * TE;
+                                    const double* dn = E[d] + ((ii[d] > 0 ? ii[d] - 1 : 0) * (LB + 2) + jj[d]) * TE;
+                                    const double* upb = E[d] + (ii[d] * (LB + 2) + jj[d] + 1) * TE;
+                                    const double* dnb = E[d] + (ii[d] * (LB + 2) + (jj[d] > 0 ? jj[d] - 1 : 0)) * TE;
+#pragma unroll
+                                    for (int t = 0; t < TE; ++t) {
+                                        dA[t] = ea2 * up[t] - (ii[d] > 0 ? ii[d] * dn[t] : 0.0);
+                                        dB[t] = eb2 * upb[t] - (jj[d] > 0 ? jj[d] * dnb[t] : 0.0);
+                                    }
+                                    const int n0 = ii[0] + jj[0], n1 = ii[1] + jj[1], n2 = ii[2] + jj[2];
+                                    double sa_, sb_;
+                                    if (d == 0) {
+                                        sa_ = bra_sum_loop<LW>(dA, e0[1], e0[2], n0 + 1, n1, n2, W);
+                                        sb_ = unit_b ? 0.0 : bra_sum_loop<LW>(dB, e0[1], e0[2], n0 + 1, n1, n2, W);
+                                    } else if (d == 1) {
+                                        sa_ = bra_sum_loop<LW>(e0[0], dA, e0[2], n0, n1 + 1, n2, W);
+                                        sb_ = unit_b ? 0.0 : bra_sum_loop<LW>(e0[0], dB, e0[2], n0, n1 + 1, n2, W);
+                                    } else {
+                                        sa_ = bra_sum_loop<LW>(e0[0], e0[1], dA, n0, n1, n2 + 1, W);
+                                        sb_ = unit_b ? 0.0 : bra_sum_loop<LW>(e0[0], e0[1], dB, n0, n1, n2 + 1, W);
+                                    }
+                                    gA[d] = fma(f, sa_, gA[d]);
+                                    gB[d] = fma(f, sb_, gB[d]);
+                                }
+                            }
+                    }
+                }
+            }
+        }
+    }
+    // the pair's atoms are the block's: one sum per component; the fitting shells' atoms per thread
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        red[d][threadIdx.x] = gA[d];
+        red[3 + d][threadIdx.x] = gB[d];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double s = 0.0;
+        for (int i = 0; i < (int)blockDim.x; ++i) s += red[threadIdx.x][i];
+        const int at = threadIdx.x < 3 ? atomA : atomB;
+        if (s != 0.0) atomicAdd(a.grad + 3 * at + threadIdx.x % 3, s);
+    }
+    if (atomC >= 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double s = gA[d] + gB[d];
+            if (s != 0.0) atomicAdd(a.grad + 3 * atomC + d, -s);
+        }
+    }
+}
+
 using Eri3Kernel = void (*)(const Eri3Args);
 int ppw(int la, int lb);
 
+using Eri3GradKernel = void (*)(const Eri3GradArgs);
+int ppw_grad(int la, int lb);
+
 // the kernel of class (la >= lb, lc), one function per fitting-shell angular momentum lc,
 // each in its own translation unit (ints3c_lc<lc>.cu) so that the classes compile in parallel
+Eri3GradKernel pick_grad_lc0(int la, int lb);
+Eri3GradKernel pick_grad_lc1(int la, int lb);
+Eri3GradKernel pick_grad_lc2(int la, int lb);
+Eri3GradKernel pick_grad_lc3(int la, int lb);
+Eri3GradKernel pick_grad_lc4(int la, int lb);
 Eri3Kernel pick_lc0(int la, int lb);
 Eri3Kernel pick_lc1(int la, int lb);
 Eri3Kernel pick_lc2(int la, int lb);
@@ -491,6 +729,24 @@ Eri3Kernel pick_pair(int la, int lb) {
         case 3 * 8 + 2: return eri3c_kernel<3, 2, LC>;
         case 3 * 8 + 3: return eri3c_kernel<3, 3, LC>;
         case 4 * 8 + 0: return eri3c_kernel<4, 0, LC>;
+        default: return nullptr;
+    }
+}
+
+template <int LC>
+Eri3GradKernel pick_grad_pair(int la, int lb) {
+    switch (la * 8 + lb) {
+        case 0 * 8 + 0: return eri3c_grad_kernel<0, 0, LC>;
+        case 1 * 8 + 0: return eri3c_grad_kernel<1, 0, LC>;
+        case 1 * 8 + 1: return eri3c_grad_kernel<1, 1, LC>;
+        case 2 * 8 + 0: return eri3c_grad_kernel<2, 0, LC>;
+        case 2 * 8 + 1: return eri3c_grad_kernel<2, 1, LC>;
+        case 2 * 8 + 2: return eri3c_grad_kernel<2, 2, LC>;
+        case 3 * 8 + 0: return eri3c_grad_kernel<3, 0, LC>;
+        case 3 * 8 + 1: return eri3c_grad_kernel<3, 1, LC>;
+        case 3 * 8 + 2: return eri3c_grad_kernel<3, 2, LC>;
+        case 3 * 8 + 3: return eri3c_grad_kernel<3, 3, LC>;
+        case 4 * 8 + 0: return eri3c_grad_kernel<4, 0, LC>;
         default: return nullptr;
     }
 }

@@ -41,10 +41,10 @@ class DeviceBasis:
         self.device = device
         self._keep = [np.ascontiguousarray(x) for x in (bs.l.astype(np.int32), bs.nprim.astype(np.int32),
                                                         bs.prim_offset.astype(np.int32), bs.exps, bs.coefs,
-                                                        bs.centers.reshape(-1))]
-        l, npr, off, ex, cf, xyz = self._keep
+                                                        bs.centers.reshape(-1), bs.atom.astype(np.int32))]
+        l, npr, off, ex, cf, xyz, at = self._keep
         h = ctypes.c_void_p()
-        rc = self.L.gdfjk_basis_create(int(device), bs.nshell, _p(l), _p(npr), _p(off), _p(ex), _p(cf), _p(xyz),
+        rc = self.L.gdfjk_basis_create(int(device), bs.nshell, _p(l), _p(npr), _p(off), _p(ex), _p(cf), _p(xyz), _p(at),
                                        int(bs.puream), ctypes.byref(h))
         if rc != 0:
             raise GdfjkError(rc, self.L.gdfjk_last_error(None).decode())
@@ -78,6 +78,27 @@ def three_index_device(aux: DeviceBasis, prim: DeviceBasis, out_ptr: int, ldo: i
     rc = aux.L.gdfjk_three_index_device(aux.h, prim.h, None if mask is None else _p(mask), int(p0), int(p1),
                                         None if col_map_ptr is None else ctypes.c_void_p(col_map_ptr), int(ldo),
                                         ctypes.c_void_p(out_ptr), None if not stream else ctypes.c_void_p(stream))
+    if rc != 0:
+        raise GdfjkError(rc, aux.L.gdfjk_last_error(None).decode())
+
+
+def three_index_grad_device(aux: DeviceBasis, prim: DeviceBasis, G3_ptr: int, ldg: int, natom: int, grad_ptr: int,
+                            shell_mask=None, col_map_ptr: int | None = None, stream: int | None = None):
+    """grad[natom][3] (device, accumulated) += sum G3[P][col(m,n)] d(P|mn)/dx over the shell
+    pairs of shell_mask (gdfjk_three_index_grad_device)."""
+    mask = None if shell_mask is None else np.ascontiguousarray(shell_mask, dtype=np.uint8)
+    rc = aux.L.gdfjk_three_index_grad_device(aux.h, prim.h, None if mask is None else _p(mask), ctypes.c_void_p(G3_ptr),
+                                             None if col_map_ptr is None else ctypes.c_void_p(col_map_ptr), int(ldg),
+                                             int(natom), ctypes.c_void_p(grad_ptr),
+                                             None if not stream else ctypes.c_void_p(stream))
+    if rc != 0:
+        raise GdfjkError(rc, aux.L.gdfjk_last_error(None).decode())
+
+
+def metric_grad_device(aux: DeviceBasis, G2_ptr: int, ldg: int, natom: int, grad_ptr: int, stream: int | None = None):
+    """grad[natom][3] (device, accumulated) += sum G2[P][Q] d(P|Q)/dx (gdfjk_metric_grad_device)."""
+    rc = aux.L.gdfjk_metric_grad_device(aux.h, ctypes.c_void_p(G2_ptr), int(ldg), int(natom), ctypes.c_void_p(grad_ptr),
+                                        None if not stream else ctypes.c_void_p(stream))
     if rc != 0:
         raise GdfjkError(rc, aux.L.gdfjk_last_error(None).decode())
 

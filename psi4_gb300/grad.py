@@ -1,10 +1,12 @@
 """RHF nuclear gradient with the density-fitted two-electron part from the GB300 engine.
 
 The engine's backward (``gdfjk_backward``) returns Gamma = dE/dB in B-space
-(B = M^-1/2 A, A = raw (P|mn), M = (P|Q)).  The host then maps it to the raw-integral
-densities psi4's DFJKGrad contracts with derivative integrals
-(psi4/src/psi4/scfgrad/jk_grad.cc:175-293, build_AB_x_terms :834-867, build_Amn_x_terms
-:868-1245):
+(B = M^-1/2 A, A = raw (P|mn), M = (P|Q)), which is mapped to the raw-integral densities
+psi4's DFJKGrad contracts with derivative integrals (psi4/src/psi4/scfgrad/jk_grad.cc:175-293,
+build_AB_x_terms :834-867, build_Amn_x_terms :868-1245) — with an engine, on the device:
+A from the engine's integral kernels, the two metric products on the tensor cores / the
+FP64 library, and both derivative-integral contractions in the engine's derivative kernels
+(gdfjk_three_index_grad_device, gdfjk_metric_grad_device); without one, on the host:
 
     3-index density  G3 = dE/dA = M^-1/2 Gamma
     2-index density  G2 = dE/dM = Frechet derivative of M -> M^-1/2 applied to
@@ -55,12 +57,63 @@ def _metric_products_device(engine, Jmhalf, Gamma, A_raw):
     return G3.cpu().numpy(), W.cpu().numpy()
 
 
-def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None):
-    """Contract Gamma (dE/dB, packed) with derivative integrals through B = M^-1/2 A.  With an
-    engine the two naux^2-sized products with the metric run on its tensor cores (FP64
-    accurate); `timings` (a dict) receives the seconds of each piece."""
+def _two_electron_gradient_device(engine, ints, df, Gamma, timings):
+    """The device path: A = (P|mn) from the integral kernels (screened function pairs zero, as
+    in the DF tensor), G3 = M^-1/2 Gamma on the tensor cores, W = Gamma A^T in FP64, the
+    Frechet derivative of M^-1/2 on the host, and both derivative contractions on the device."""
     import time
 
+    import torch
+
+    from .device_init import DeviceBasis, metric_grad_device, three_index_device, three_index_grad_device
+
+    dev = torch.device("cuda", engine.device)
+    sp = df.sparsity
+    naux, npair = Gamma.shape
+    natom = ints.mol.natom
+    t = time.perf_counter()
+    pd, ad = DeviceBasis(ints.primary, engine.device), DeviceBasis(ints.aux, engine.device)
+    A = torch.zeros((naux, npair), dtype=torch.float64, device=dev)
+    three_index_device(ad, pd, A.data_ptr(), npair, shell_mask=sp.shell_mask)
+    r, c = np.tril_indices(df.nbf)
+    A *= torch.from_numpy(sp.pair_mask[r, c].astype(np.float64)).to(dev)
+    torch.cuda.synchronize(dev)
+    t1 = time.perf_counter()
+    Gd = torch.from_numpy(np.ascontiguousarray(Gamma)).to(dev)
+    Jm = torch.from_numpy(np.ascontiguousarray(df.Jmhalf)).to(dev)
+    G3 = torch.empty_like(Gd)
+    engine.gemm(Jm.data_ptr(), naux, Gd.data_ptr(), npair, G3.data_ptr(), npair, naux, npair, naux)
+    W = (Gd @ A.T).cpu().numpy()
+    del A, Gd, Jm
+    t2 = time.perf_counter()
+    G2 = metric_power_frechet(df.metric, W)
+    t3 = time.perf_counter()
+    g = torch.zeros((natom, 3), dtype=torch.float64, device=dev)
+    three_index_grad_device(ad, pd, G3.data_ptr(), npair, natom, g.data_ptr(), shell_mask=sp.shell_mask)
+    t4 = time.perf_counter()
+    G2d = torch.from_numpy(np.ascontiguousarray(G2)).to(dev)
+    metric_grad_device(ad, G2d.data_ptr(), naux, natom, g.data_ptr())
+    out = g.cpu().numpy()
+    t5 = time.perf_counter()
+    pd.close()
+    ad.close()
+    if timings is not None:
+        timings.update({"three_index_s": t1 - t, "metric_products_s": t2 - t1, "metric_frechet_s": t3 - t2,
+                        "three_index_derivative_contraction_s": t4 - t3, "metric_derivative_contraction_s": t5 - t4,
+                        "metric_products_on": "tensor cores (G3) and the FP64 library (W)",
+                        "integrals_and_derivative_contractions_on": "device"})
+    return out
+
+
+def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None):
+    """Contract Gamma (dE/dB, packed) with derivative integrals through B = M^-1/2 A.  With an
+    engine everything but the Frechet derivative of M^-1/2 runs on its device (integrals,
+    metric products, derivative contractions); `timings` (a dict) receives the seconds of each
+    piece."""
+    import time
+
+    if engine is not None and A_raw is None:
+        return _two_electron_gradient_device(engine, ints, df, Gamma, timings)
     t = time.perf_counter()
     if A_raw is None:
         A_raw = ints.three_index(shell_mask=df.sparsity.shell_mask)

@@ -17,7 +17,7 @@ def _create(L, l, puream=1):
     xyz = np.zeros(3 * n)
     h = ctypes.c_void_p()
     p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
-    return L.gdfjk_basis_create(0, n, p(la), p(npr), p(off), p(ex), p(cf), p(xyz), puream, ctypes.byref(h)), h
+    return L.gdfjk_basis_create(0, n, p(la), p(npr), p(off), p(ex), p(cf), p(xyz), None, puream, ctypes.byref(h)), h
 
 
 def test_basis_create_rejects_h_shells(jk_built):
@@ -33,3 +33,5 @@ def test_three_index_rejects_null_bases(jk_built):
     assert rc == _jkabi.GDFJK_ERR_ARG
     rc = L.gdfjk_metric_device(None, 0, 1, 1, None, None)
     assert rc == _jkabi.GDFJK_ERR_ARG
+    assert L.gdfjk_three_index_grad_device(None, None, None, None, None, 1, 1, None, None) == _jkabi.GDFJK_ERR_ARG
+    assert L.gdfjk_metric_grad_device(None, None, 1, 1, None, None) == _jkabi.GDFJK_ERR_ARG
