@@ -922,6 +922,32 @@ def measure_scf_device_B(cfg, dev):
     out["host_seconds_per_iteration"] = {
         "fp64_emulated": (em["seconds"] - em["jk_seconds"]) / em["iterations"],
         "precision_form": (pf["seconds"] - pf["jk_seconds"]) / pf["iterations"]}
+    if screened:
+        # the analytic gradient at the precision form's converged orbitals, (Q|mi) recomputed in
+        # the aux-batched backward, every naux x pairs array over the significant pairs
+        try:
+            from psi4_gb300.grad import one_electron_gradient, two_electron_gradient_screened
+
+            tm = {}
+            used_before = used[0]
+            used[0] = 0
+            tg = time.perf_counter()
+            g2 = two_electron_gradient_screened(dd.engine, ints, dd.sparsity, dd.metric, dd.Jmhalf,
+                                                np.ascontiguousarray(r_pf.C[:, :nocc]), timings=tm,
+                                                callback=sample_memory)
+            t2e = time.perf_counter() - tg
+            t1 = time.perf_counter()
+            g1 = one_electron_gradient(mol, ints, r_pf)
+            t1e = time.perf_counter() - t1
+            g = g1 + g2
+            out["gradient"] = {"seconds": t2e + t1e, "two_electron_device_s": t2e, "one_electron_host_s": t1e,
+                               "two_electron_pieces_s": tm, "max_abs_gradient": float(np.abs(g).max()),
+                               "translational_invariance_max_abs_sum": float(np.abs(g.sum(0)).max()),
+                               "peak_device_memory_gb": used[0] / 1e9,
+                               "note": "the tensor-core forms' copies of B are released for the gradient"}
+            used[0] = max(used[0], used_before)
+        except Exception as ex:  # reported, not hidden
+            out["gradient"] = {"unavailable": str(ex)[:300]}
     jk.finalize()
     return out
 

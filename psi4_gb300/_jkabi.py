@@ -29,6 +29,7 @@ SIGNATURES = {
     "gdfjk_compute_incremental": (I, [P, P, I, I, P, I, I, I, I, P, P]),
     "gdfjk_compute_incremental_device": (I, [P, P, I, I, P, I, I, I, I, P, P]),
     "gdfjk_backward": (I, [P, P, I, I, P, P, P, P, I]),
+    "gdfjk_backward_gamma_device": (I, [P, P, I, I, P, P, P, ctypes.c_int64, P, I]),
     "gdfjk_query_memory": (I, [I, I, I, I, ctypes.POINTER(SZ)]),
     "gdfjk_last_timings": (I, [P, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(D)]),
     "gdfjk_synchronize": (I, [P, D]),

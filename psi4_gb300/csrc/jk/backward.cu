@@ -83,14 +83,16 @@ void launch_gemm_nn_fp64(int M, size_t N, int K, const double* A, size_t lda, co
     gemm_nn_fp64_kernel<<<grid, 128, 0, stream>>>(K, A, lda, Bm, ldb, alpha, beta, out, ldo);
 }
 
-// Gamma for the stored tile t and auxiliary index Q (blockIdx = (t, Q)), packed output
-// out[Q*npair + m(m+1)/2 + n] for m >= n (x2 off the diagonal).  Y[m][Q][i], C[m][i].
+// Gamma for the stored tile t and auxiliary index Q (blockIdx = (t, Q)), written to
+// out[Q*ldo + col] with col = m(m+1)/2 + n for m >= n, or col_map[m(m+1)/2 + n] (entries < 0
+// are not stored), x2 off the diagonal.  Y[m][Q][i], C[m][i]; dq, gq indexed by the same Q.
 __global__ void __launch_bounds__(256) gamma_kernel(const double* __restrict__ Y, const double* __restrict__ C,
                                                     const double* __restrict__ gJ, const double* __restrict__ D,
                                                     const double* __restrict__ dq, const double* __restrict__ gq,
                                                     int naux, int nbf, int nbf_pad, int nocc_pad,
                                                     const int* __restrict__ tI, const int* __restrict__ tJ,
-                                                    double* __restrict__ out) {
+                                                    double* __restrict__ out, size_t ldo,
+                                                    const long long* __restrict__ col_map) {
     __shared__ double Ym[16][TILE + 1], Cm[16][TILE + 1], Yn[16][TILE + 1], Cn[16][TILE + 1];
     int t = blockIdx.x, Q = blockIdx.y;
     int I = tI[t], J = tJ[t];
@@ -119,7 +121,6 @@ __global__ void __launch_bounds__(256) gamma_kernel(const double* __restrict__ Y
         __syncthreads();
     }
     double d = dq[Q], g = gq[Q];
-    size_t npair = (size_t)nbf * (nbf + 1) / 2;
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -128,16 +129,23 @@ __global__ void __launch_bounds__(256) gamma_kernel(const double* __restrict__ Y
             if (m >= nbf || n >= nbf || m < n) continue;
             size_t mn = (size_t)m * nbf_pad + n;
             double val = acc[u][v] + gJ[mn] * d + g * D[mn];
-            out[(size_t)Q * npair + (size_t)m * (m + 1) / 2 + n] = (m > n ? 2.0 : 1.0) * val;
+            long long col = (long long)m * (m + 1) / 2 + n;
+            if (col_map) {
+                col = col_map[col];
+                if (col < 0) continue;
+            }
+            out[(size_t)Q * ldo + (size_t)col] = (m > n ? 2.0 : 1.0) * val;
         }
 }
 
 void launch_gamma(const double* Y, const double* C, const double* gJ, const double* D, const double* dq,
                   const double* gq, int naux, int nbf, int nbf_pad, int nocc_pad, const TileLayout& L, double* out,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, size_t ldo, const long long* col_map) {
     if (L.ntiles == 0 || naux == 0) return;
+    if (ldo == 0) ldo = (size_t)nbf * (nbf + 1) / 2;
     dim3 grid(L.ntiles, naux);
-    gamma_kernel<<<grid, 256, 0, stream>>>(Y, C, gJ, D, dq, gq, naux, nbf, nbf_pad, nocc_pad, L.tI, L.tJ, out);
+    gamma_kernel<<<grid, 256, 0, stream>>>(Y, C, gJ, D, dq, gq, naux, nbf, nbf_pad, nocc_pad, L.tI, L.tJ, out, ldo,
+                                           col_map);
 }
 
 // out[e] = alpha * sum_{b < nblk} part[b*n + e] + beta * out[e]   (fixed order)

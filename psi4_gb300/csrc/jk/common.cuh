@@ -127,9 +127,11 @@ void launch_copy_out(const double* src, int nbf, int nbf_pad, double* dst, cudaS
 void launch_pad_sym(const double* g, int nbf, int nbf_pad, double* out, cudaStream_t stream);
 void launch_gemm_nn_fp64(int M, size_t N, int K, const double* A, size_t lda, const double* Bm, size_t ldb, double alpha,
                          double beta, double* out, size_t ldo, cudaStream_t stream);
+// Gamma rows for the naux aux functions of Y (row Q at out + Q*ldo, ldo = 0: nbf(nbf+1)/2),
+// packed-triangle columns or col_map's
 void launch_gamma(const double* Y, const double* C, const double* gJ, const double* D, const double* dq,
                   const double* gq, int naux, int nbf, int nbf_pad, int nocc_pad, const TileLayout& L, double* out,
-                  cudaStream_t stream);
+                  cudaStream_t stream, size_t ldo = 0, const long long* col_map = nullptr);
 void launch_reduce_blocks(const double* part, int nblk, size_t n, double alpha, double beta, double* out,
                           cudaStream_t stream);
 void launch_copy_rect(const double* src, int nbf, int nocc, int nocc_pad, double* dst, int ldd, cudaStream_t stream);

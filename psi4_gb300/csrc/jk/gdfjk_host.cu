@@ -978,6 +978,83 @@ int gdfjk_backward(gdfjk_t h, const double* C, int nocc, int ldc, const double* 
     return GDFJK_OK;
 }
 
+int gdfjk_backward_gamma_device(gdfjk_t h, const double* C, int nocc, int ldc, const double* gJ, const double* gK,
+                                const int64_t* col_map, int64_t ldg, double* Gamma, int batch_q) {
+    if (!h) return set_err(h, GDFJK_ERR_ARG, "backward_gamma: null handle");
+    if (!h->B_ready) return set_err(h, GDFJK_ERR_STATE, "backward_gamma: B has not been uploaded");
+    const int nbf = h->nbf, nbf_pad = h->nbf_pad, naux = h->naux;
+    const size_t npair = (size_t)nbf * (nbf + 1) / 2;
+    if (nocc <= 0 || !C || ldc < nocc || !gJ || !gK || !Gamma || batch_q < 0 ||
+        ldg < (int64_t)(col_map ? 1 : npair))
+        return set_err(h, GDFJK_ERR_ARG, "backward_gamma: bad C / nocc / ldc / ldg or null argument");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const int nocc_pad = round_up(nocc, 32);
+    int rc = ensure_workspace(h, nocc_pad, false, false);
+    if (rc) return rc;
+    const size_t np2 = (size_t)nbf_pad * nbf_pad;
+    if (!h->gJp || !h->gKp || !h->Jg || !h->gq || !h->Dw2 || !h->Jgt) {
+        if ((rc = dalloc(h, &h->gJp, np2)) || (rc = dalloc(h, &h->gKp, np2)) || (rc = dalloc(h, &h->Jg, np2)) ||
+            (rc = dalloc(h, &h->gq, (size_t)naux)) || (rc = dalloc(h, &h->Dw2, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS)) ||
+            (rc = dalloc(h, &h->Jgt, (size_t)std::max(h->ntiles, 1) * TILE_ELEMS)))
+            return rc;
+    }
+    // aux batch: X_b and Y_b (nbf_pad x qb x nocc_pad each) within GDFJK_BW_BATCH_GB (default 16 GB)
+    const double per_q = 2.0 * nbf_pad * nocc_pad * 8.0;
+    int qb = batch_q;
+    if (qb == 0) {
+        const char* e = getenv("GDFJK_BW_BATCH_GB");
+        double gb = e ? atof(e) : 16.0;
+        if (!(gb > 0.0)) gb = 16.0;
+        qb = (int)std::max(1.0, std::floor(gb * 1e9 / per_q));
+    }
+    qb = std::max(1, std::min({qb, naux, 65535}));
+    double *Xb = nullptr, *Yb = nullptr;
+    auto release = [&]() {
+        if (Xb) cudaFree(Xb);
+        if (Yb) cudaFree(Yb);
+        Xb = Yb = nullptr;
+    };
+    const size_t be = (size_t)nbf_pad * qb * nocc_pad;
+    if ((rc = dalloc(h, &Xb, be)) || (rc = dalloc(h, &Yb, be))) {
+        release();
+        return rc;
+    }
+    TileLayout L = layout_of(h);
+    launch_pad_C(C, nbf, nocc, ldc, nbf_pad, nocc_pad, h->Cl, s);
+    launch_density(h->Cl, h->Cl, nbf_pad, nocc_pad, h->D, s);
+    launch_weighted_density_tiles(h->D, nbf_pad, L, h->Dw, s);
+    launch_j_pass1(h->B, h->Dw, naux, L, h->dq, s);
+    launch_pad_sym(gJ, nbf, nbf_pad, h->gJp, s);
+    launch_pad_sym(gK, nbf, nbf_pad, h->gKp, s);
+    launch_weighted_density_tiles(h->gJp, nbf_pad, L, h->Dw2, s);
+    launch_j_pass1(h->B, h->Dw2, naux, L, h->gq, s);
+    if (cudaMemsetAsync(Gamma, 0, (size_t)naux * ldg * 8, s) != cudaSuccess) {
+        release();
+        return set_err(h, GDFJK_ERR_CUDA, "backward_gamma: clearing Gamma failed");
+    }
+    if (!h->oz) h->oz = oz_create();
+    for (int q0 = 0; q0 < naux; q0 += qb) {
+        const int nq = std::min(qb, naux - q0);
+        const size_t kd = (size_t)nq * nocc_pad;
+        // X_b[m][Q][i] = sum_n B_Q,mn C_ni over this batch's rows of B
+        launch_k_transform_fp64(h->B + (size_t)q0 * h->ntiles * TILE_ELEMS, h->Cl, nq, nbf_pad, nocc_pad, L, Xb, s);
+        // Y_b = gK X_b on the tensor cores (the metric contraction's FP64-accurate digit product)
+        rc = oz_gemm(h->oz, h->gKp, (size_t)nbf_pad, Xb, kd, Yb, kd, nbf_pad, (int)kd, nbf_pad, 0, s, h->err);
+        if (rc) {
+            release();
+            return set_err(h, rc, "backward_gamma: " + h->err);
+        }
+        launch_gamma(Yb, h->Cl, h->gJp, h->D, h->dq + q0, h->gq + q0, nq, nbf, nbf_pad, nocc_pad, L,
+                     Gamma + (size_t)q0 * ldg, s, (size_t)ldg, reinterpret_cast<const long long*>(col_map));
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    release();
+    if (e != cudaSuccess) return set_err(h, GDFJK_ERR_CUDA, std::string("backward_gamma: ") + cudaGetErrorString(e));
+    return check_device_flag(h);
+}
+
 int gdfjk_debug_refuse_allocations(int after, int count) {
     if (after < 0 || count < 0) return set_err(nullptr, GDFJK_ERR_ARG, "debug_refuse_allocations: negative count");
     std::lock_guard<std::mutex> lock(g_alloc_mutex);

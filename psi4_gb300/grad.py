@@ -38,6 +38,104 @@ def metric_power_frechet(M, W, power=-0.5, condition=1e-10):
     return V @ (Lm * (V.T @ Ws @ V)) @ V.T
 
 
+def metric_power_frechet_device(Md, Wd, power=-0.5, condition=1e-10):
+    """metric_power_frechet on device arrays (the library's FP64 eigensolver and GEMMs), for
+    large fitting sets; same truncation and divided differences."""
+    import torch
+
+    w, V = torch.linalg.eigh(Md)
+    max_a = torch.maximum(w[-1].abs(), w[0].abs())
+    aw = w.abs()
+    keep = aw >= condition * max_a if power < 0 else torch.ones_like(w, dtype=torch.bool)
+    safe = torch.where(keep, aw, torch.ones_like(aw))
+    f = torch.where(keep, safe ** power, torch.zeros_like(w))
+    fp = torch.where(keep, power * safe ** (power - 1.0), torch.zeros_like(w))
+    dl = w[:, None] - w[None, :]
+    same = dl.abs() <= 1e-14 * torch.clamp(w[:, None].abs(), min=1.0)
+    Lm = torch.where(same, 0.5 * (fp[:, None] + fp[None, :]), (f[:, None] - f[None, :]) / torch.where(same, torch.ones_like(dl), dl))
+    Ws = 0.5 * (Wd + Wd.T)
+    return V @ (Lm * (V.T @ Ws @ V)) @ V.T
+
+
+def two_electron_gradient_screened(engine, ints, sp, metric, Jmhalf, C, timings=None, batch_q=0, callback=None):
+    """The two-electron gradient with every naux x pairs array kept over the significant pairs
+    only (the layout of device_init.build_device_B_screened), for systems whose dense triangle
+    would not fit (C100H202): Gamma = dE/dB from the engine's batched backward with (Q|mi)
+    recomputed (gdfjk_backward_gamma_device), G3 = M^-1/2 Gamma and W = Gamma A^T on the
+    tensor cores (FP64-accurate digit products; W's digit error moved the (H2O)_16 gradient by
+    5e-8 Eh/bohr), A from the integral kernels, the Frechet derivative of M^-1/2 on the device,
+    and the derivative contractions in the derivative kernels.  C: occupied orbitals (host);
+    the tensor-core forms' copies of B are released first (rebuilt by the next build).
+    callback() is called after each large piece (memory sampling)."""
+    import time
+
+    import torch
+
+    from .device_init import DeviceBasis, metric_grad_device, three_index_device, three_index_grad_device
+
+    dev = torch.device("cuda", engine.device)
+    nbf, nocc = C.shape
+    naux = metric.shape[0]
+    natom = ints.mol.natom
+    tm = {}
+    t = time.perf_counter()
+    r, c = np.tril_indices(nbf)
+    sig = np.flatnonzero(sp.pair_mask[r, c])
+    nsig = sig.size
+    col_map = np.full(r.size, -1, dtype=np.int64)
+    col_map[sig] = np.arange(nsig, dtype=np.int64)
+    col_d = torch.from_numpy(col_map).to(dev)
+    engine.trim()
+    Cd = torch.from_numpy(np.ascontiguousarray(C)).to(dev)
+    D = Cd @ Cd.T
+    gJ, gK = 2.0 * D, -D
+    G = torch.empty((naux, nsig), dtype=torch.float64, device=dev)
+    engine.backward_gamma_device(Cd.data_ptr(), nocc, nocc, gJ.data_ptr(), gK.data_ptr(), G.data_ptr(), nsig,
+                                 col_map_ptr=col_d.data_ptr(), batch_q=batch_q)
+    del D, gJ, gK
+    if callback:
+        callback()
+    t1 = time.perf_counter()
+    Jm = torch.from_numpy(np.ascontiguousarray(Jmhalf)).to(dev)
+    G3 = torch.empty_like(G)
+    engine.gemm(Jm.data_ptr(), naux, G.data_ptr(), nsig, G3.data_ptr(), nsig, naux, nsig, naux)
+    del Jm
+    t2 = time.perf_counter()
+    pd, ad = DeviceBasis(ints.primary, engine.device), DeviceBasis(ints.aux, engine.device)
+    A = torch.zeros_like(G)
+    three_index_device(ad, pd, A.data_ptr(), nsig, shell_mask=sp.shell_mask, col_map_ptr=col_d.data_ptr())
+    if callback:
+        callback()
+    t3 = time.perf_counter()
+    W = torch.empty((naux, naux), dtype=torch.float64, device=dev)
+    engine.gemm(G.data_ptr(), nsig, A.data_ptr(), nsig, W.data_ptr(), naux, naux, naux, nsig, transb=True)
+    del A, G
+    torch.cuda.empty_cache()
+    t4 = time.perf_counter()
+    Md = torch.from_numpy(np.ascontiguousarray(metric)).to(dev)
+    G2 = metric_power_frechet_device(Md, W)
+    del Md, W
+    torch.cuda.synchronize(dev)
+    t5 = time.perf_counter()
+    g = torch.zeros((natom, 3), dtype=torch.float64, device=dev)
+    three_index_grad_device(ad, pd, G3.data_ptr(), nsig, natom, g.data_ptr(), shell_mask=sp.shell_mask,
+                            col_map_ptr=col_d.data_ptr())
+    t6 = time.perf_counter()
+    metric_grad_device(ad, G2.data_ptr(), naux, natom, g.data_ptr())
+    out = g.cpu().numpy()
+    t7 = time.perf_counter()
+    del G3, G2, col_d
+    pd.close()
+    ad.close()
+    torch.cuda.empty_cache()
+    if timings is not None:
+        timings.update({"backward_gamma_s": t1 - t, "metric_product_G3_s": t2 - t1, "three_index_s": t3 - t2,
+                        "metric_product_W_s": t4 - t3, "metric_frechet_device_s": t5 - t4,
+                        "three_index_derivative_contraction_s": t6 - t5, "metric_derivative_contraction_s": t7 - t6,
+                        "significant_pairs": int(nsig)})
+    return out
+
+
 def _metric_products_device(engine, Jmhalf, Gamma, A_raw):
     """G3 = M^-1/2 Gamma on the tensor cores to FP64 accuracy (gdfjk_gemm_device, the metric
     contraction's digit product) and W = Gamma A^T as a plain FP64 library product on the same
@@ -137,6 +235,20 @@ def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None
                         "three_index_derivative_contraction_s": t4 - t3, "metric_derivative_contraction_s": t5 - t4,
                         "metric_products_on": "tensor cores" if engine is not None else "host"})
     return g3 + g2
+
+
+def one_electron_gradient(mol, ints, scf):
+    """E_nuc^x + 2 D.(T^x + V^x) - 2 W.S^x (host provider), D and W from the occupied orbitals."""
+    nocc = scf.nocc
+    C = scf.C[:, :nocc]
+    eps = scf.eps[:nocc]
+    D = C @ C.T
+    W = (C * eps) @ C.T
+    g = mol.nuclear_repulsion_grad()
+    g += 2.0 * ints.kinetic_grad(D)
+    g += 2.0 * ints.potential_grad(D)
+    g -= 2.0 * ints.overlap_grad(W)
+    return g
 
 
 def rhf_gradient(mol, ints, df, scf, Gamma, engine=None, timings=None):

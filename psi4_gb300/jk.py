@@ -175,6 +175,13 @@ class DFJKEngine:
         self._check(self.L.gdfjk_backward(self.h, _p(C), nocc, max(nocc, 1), _p(gJ), _p(gK), _p(dC), _p(G), 0))
         return dC, G
 
+    def backward_gamma_device(self, C_ptr, nocc, ldc, gJ_ptr, gK_ptr, G_ptr, ldg, col_map_ptr=None, batch_q=0):
+        """gdfjk_backward_gamma_device: Gamma = dE/dB alone over aux batches, into a device
+        array (packed-triangle columns or col_map's), device C / gJ / gK."""
+        vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
+        self._check(self.L.gdfjk_backward_gamma_device(self.h, vp(C_ptr), int(nocc), int(ldc), vp(gJ_ptr), vp(gK_ptr),
+                                                       vp(col_map_ptr), int(ldg), vp(G_ptr), int(batch_q)))
+
     def backward_device(self, C_ptr, nocc, ldc, gJ_ptr, gK_ptr, dC_ptr, G_ptr):
         vp = lambda x: None if x is None else ctypes.c_void_p(int(x))
         self._check(self.L.gdfjk_backward(self.h, vp(C_ptr), int(nocc), int(ldc), vp(gJ_ptr), vp(gK_ptr), vp(dC_ptr),
