@@ -926,7 +926,7 @@ def measure_scf_device_B(cfg, dev):
         # the analytic gradient at the precision form's converged orbitals, (Q|mi) recomputed in
         # the aux-batched backward, every naux x pairs array over the significant pairs
         try:
-            from psi4_gb300.grad import one_electron_gradient, two_electron_gradient_screened
+            from psi4_gb300.grad import one_electron_gradient_device, two_electron_gradient_screened
 
             tm = {}
             used_before = used[0]
@@ -934,13 +934,13 @@ def measure_scf_device_B(cfg, dev):
             tg = time.perf_counter()
             g2 = two_electron_gradient_screened(dd.engine, ints, dd.sparsity, dd.metric, dd.Jmhalf,
                                                 np.ascontiguousarray(r_pf.C[:, :nocc]), timings=tm,
-                                                callback=sample_memory)
+                                                callback=sample_memory, metric_eig=dd.metric_eig)
             t2e = time.perf_counter() - tg
             t1 = time.perf_counter()
-            g1 = one_electron_gradient(mol, ints, r_pf)
+            g1 = one_electron_gradient_device(mol, ints, r_pf, device=dev.index or 0)
             t1e = time.perf_counter() - t1
             g = g1 + g2
-            out["gradient"] = {"seconds": t2e + t1e, "two_electron_device_s": t2e, "one_electron_host_s": t1e,
+            out["gradient"] = {"seconds": t2e + t1e, "two_electron_device_s": t2e, "one_electron_s": t1e,
                                "two_electron_pieces_s": tm, "max_abs_gradient": float(np.abs(g).max()),
                                "translational_invariance_max_abs_sum": float(np.abs(g.sum(0)).max()),
                                "peak_device_memory_gb": used[0] / 1e9,

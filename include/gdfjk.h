@@ -141,6 +141,15 @@ int gdfjk_three_index_grad_device(gdfjk_basis_t aux, gdfjk_basis_t prim, const u
                                   void* stream);
 int gdfjk_metric_grad_device(gdfjk_basis_t aux, const double* G2, int64_t ldg, int natom, double* grad, void* stream);
 
+/* The nuclear-attraction part of the one-electron gradient (psi4's potential derivative
+ * integrals contracted with the density, scf_grad.cc:196-220): grad[natom][3] (device,
+ * accumulated) += sum over m >= n of Dp[m(m+1)/2+n] d(V_mn)/dx, V_mn = -sum_C Z_C (m|1/r_C|n),
+ * Dp a device packed triangle with the off-diagonal entries doubled (so that the sum is
+ * sum_mn D_mn dV_mn for a symmetric D); Z and xyz (bohr) host arrays of natom charges and
+ * positions.  The same derivative class kernels with point charges for the fitting shells. */
+int gdfjk_potential_grad_device(gdfjk_basis_t prim, const double* Dp, int natom, const double* Z, const double* xyz,
+                                double* grad, void* stream);
+
 /* The metric contraction B = J^-1/2 (P|mn) on the tensor cores, to FP64 accuracy (the
  * emulated-FP64 digit products of GDFJK_EMULATED): replaces the naux x naux DGEMM of
  * DFHelper::contract_metric_AO_core_symm (dfhelper.cc:1653-1678) called from

@@ -23,6 +23,7 @@ SIGNATURES = {
     "gdfjk_metric_device": (I, [P, I, I, ctypes.c_int64, P, P]),
     "gdfjk_three_index_grad_device": (I, [P, P, P, P, P, ctypes.c_int64, I, P, P]),
     "gdfjk_metric_grad_device": (I, [P, P, ctypes.c_int64, I, P, P]),
+    "gdfjk_potential_grad_device": (I, [P, P, I, P, P, P, P]),
     "gdfjk_compute": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_device": (I, [P, P, P, I, I, I, P, P, P]),
     "gdfjk_compute_wK": (I, [P, P, P, P, I, I, I, P]),

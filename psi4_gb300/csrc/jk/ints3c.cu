@@ -456,6 +456,53 @@ int gdfjk_three_index_grad_device(gdfjk_basis_t aux, gdfjk_basis_t prim, const u
     return rc ? report_error(rc, err) : GDFJK_OK;
 }
 
+int gdfjk_potential_grad_device(gdfjk_basis_t prim, const double* Dp, int natom, const double* Z, const double* xyz,
+                                double* grad, void* stream) {
+    if (!prim || !Dp || !Z || !xyz || !grad) return report_error(GDFJK_ERR_ARG, "potential_grad_device: null argument");
+    if (prim->maxl > ints::MAXL_PAIR)
+        return report_error(GDFJK_ERR_ARG, "potential_grad_device: primary shells above f are not supported");
+    if (natom <= 0 || !ints::atoms_valid(prim, natom))
+        return report_error(GDFJK_ERR_ARG, "potential_grad_device: the basis needs atom indices below natom");
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(prim->device);
+    const int nsp = prim->nshell;
+    std::vector<int2> pairs[(ints::MAXL_PAIR + 1) * (ints::MAXL_PAIR + 1)];
+    for (int M = 0; M < nsp; ++M)
+        for (int N = 0; N <= M; ++N) {
+            const int lm = prim->l[M], ln = prim->l[N];
+            const int2 pr = lm >= ln ? make_int2(M, N) : make_int2(N, M);
+            pairs[std::max(lm, ln) * (ints::MAXL_PAIR + 1) + std::min(lm, ln)].push_back(pr);
+        }
+    std::vector<int> fits[ints::MAXL_FIT + 1];
+    for (int a = 0; a < natom; ++a) fits[0].push_back(a);
+    double* dZ = nullptr;
+    std::string err;
+    int rc = GDFJK_OK;
+    if (engine_malloc((void**)&dZ, (size_t)natom * 4 * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaSetDevice(cur);
+        return report_error(GDFJK_ERR_OOM, "potential_grad_device: device allocation refused");
+    }
+    cudaMemcpy(dZ, Z, (size_t)natom * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dZ + natom, xyz, (size_t)natom * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    ints::Eri3GradArgs base{};
+    base.pure_ab = prim->puream;
+    base.pure_c = 0;
+    base.G = Dp;
+    base.ldg = 0;  // every charge reads the same density row
+    base.col_map = nullptr;
+    base.grad = grad;
+    base.metric = 0;
+    base.charges = dZ;
+    base.charge_xyz = dZ + natom;
+    rc = ints::run_grad_classes(prim, prim, pairs, (int)(sizeof(pairs) / sizeof(pairs[0])), fits, base,
+                                (cudaStream_t)stream, err);
+    cudaFree(dZ);
+    cudaSetDevice(cur);
+    return rc ? report_error(rc, err) : GDFJK_OK;
+}
+
 int gdfjk_metric_grad_device(gdfjk_basis_t aux, const double* G2, int64_t ldg, int natom, double* grad, void* stream) {
     if (!aux || !G2 || !grad) return report_error(GDFJK_ERR_ARG, "metric_grad_device: null argument");
     if (ldg < aux->nbf) return report_error(GDFJK_ERR_ARG, "metric_grad_device: leading dimension below naux");

@@ -488,6 +488,10 @@ struct Eri3GradArgs {
     const double* boys;
     const double* pure;
     int metric;                // 1: G[P][Q] against (P|Q), the pair being (Q, unit)
+    // point charges instead of fitting shells (nullable): fits index atoms with charge
+    // charges[i] at charge_xyz[3i..]; the nuclear attraction -Z (mn|1/r_C) (lc = 0)
+    const double* charges;
+    const double* charge_xyz;
 };
 
 // adjoint of to_pure: pure components in the first 2l+1 slots of the index -> all ncart slots
@@ -550,17 +554,18 @@ __global__ void __launch_bounds__(ERI_THREADS) eri3c_grad_kernel(const Eri3GradA
     const int ci = blockIdx.y * blockDim.x + threadIdx.x;
     double gA[3] = {0.0, 0.0, 0.0}, gB[3] = {0.0, 0.0, 0.0};
     int atomC = -1;
+    const bool point = a.charges != nullptr;
     if (ci < a.nfit) {
         const int sc = a.fits[ci];
-        atomC = a.cs.atom[sc];
+        atomC = point ? sc : a.cs.atom[sc];
         if (!(atomA == atomB && atomB == atomC)) {
             // the density block in solid harmonics, then in Cartesian components
             double g[NA * NB * NC];
 #pragma unroll 1
             for (int k = 0; k < NA * NB * NC; ++k) g[k] = 0.0;
             const int na = a.pure_ab ? 2 * LA + 1 : NA, nb = unit_b ? 1 : (a.pure_ab ? 2 * LB + 1 : NB);
-            const int nc = a.pure_c ? 2 * LC + 1 : NC;
-            const int fa = a.ab.foff[sa], fb = unit_b ? 0 : a.ab.foff[sb], fc = a.cs.foff[sc];
+            const int nc = point ? 1 : (a.pure_c ? 2 * LC + 1 : NC);
+            const int fa = a.ab.foff[sa], fb = unit_b ? 0 : a.ab.foff[sb], fc = point ? 0 : a.cs.foff[sc];
 #pragma unroll 1
             for (int q = 0; q < nc; ++q) {
                 const double* row = a.G + (size_t)(fc + q) * a.ldg;
@@ -583,13 +588,13 @@ __global__ void __launch_bounds__(ERI_THREADS) eri3c_grad_kernel(const Eri3GradA
                     }
                 }
             }
-            if (a.pure_c) from_pure<LC, NA * NB, NC, 1, 1>(a.pure, g);
+            if (a.pure_c && !point) from_pure<LC, NA * NB, NC, 1, 1>(a.pure, g);
             if (a.pure_ab) {
                 from_pure<LB, NA, NB * NC, NC, NC>(a.pure, g);
                 from_pure<LA, 1, 0, NB * NC, NB * NC>(a.pure, g);
             }
-            const double* Cc = a.cs.xyz + 3 * sc;
-            const int npc = a.cs.nprim[sc], pc0 = a.cs.poff[sc];
+            const double* Cc = point ? a.charge_xyz + 3 * sc : a.cs.xyz + 3 * sc;
+            const int npc = point ? 1 : a.cs.nprim[sc], pc0 = point ? 0 : a.cs.poff[sc];
             constexpr double TWO_PI_52 = 34.986836655249725;
             constexpr double SGN = (LC & 1) ? -1.0 : 1.0;
 #pragma unroll 1
@@ -599,14 +604,16 @@ __global__ void __launch_bounds__(ERI_THREADS) eri3c_grad_kernel(const Eri3GradA
                 const double* E[3] = {w + 7, w + 7 + ED, w + 7 + 2 * ED};
 #pragma unroll 1
                 for (int kc = 0; kc < npc; ++kc) {
-                    const double c = a.cs.exps[pc0 + kc];
-                    const double pc = p + c, alpha = p * c / pc;
+                    // a fitting Gaussian of exponent c, or a point charge (alpha = p, 2 pi / p)
+                    const double c = point ? 1.0 : a.cs.exps[pc0 + kc];
+                    const double pc = p + c, alpha = point ? p : p * c / pc;
                     const double X = w[1] - Cc[0], Y = w[2] - Cc[1], Z = w[3] - Cc[2];
                     double F[L + 1];
                     boys<L>(a.boys, alpha * (X * X + Y * Y + Z * Z), F);
                     double R[NTL];
                     hermite_r<L, false>(alpha, X, Y, Z, F, R);
-                    const double pref = SGN * TWO_PI_52 / (p * c * sqrt(pc)) * w[4] * a.cs.coefs[pc0 + kc];
+                    const double pref = point ? -6.283185307179586 / p * w[4] * a.charges[sc]
+                                              : SGN * TWO_PI_52 / (p * c * sqrt(pc)) * w[4] * a.cs.coefs[pc0 + kc];
                     double Ec[(LC + 1) * (LC + 1)];
 #pragma unroll
                     for (int q = 0; q < (LC + 1) * (LC + 1); ++q) Ec[q] = 0.0;

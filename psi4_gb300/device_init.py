@@ -95,6 +95,18 @@ def three_index_grad_device(aux: DeviceBasis, prim: DeviceBasis, G3_ptr: int, ld
         raise GdfjkError(rc, aux.L.gdfjk_last_error(None).decode())
 
 
+def potential_grad_device(prim: DeviceBasis, Dp_ptr: int, mol: Molecule, grad_ptr: int, stream: int | None = None):
+    """grad[natom][3] (device, accumulated) += sum_{m>=n} Dp[m(m+1)/2+n] dV_mn/dx, the nuclear
+    attraction's derivative integrals with the molecule's point charges
+    (gdfjk_potential_grad_device); Dp: device packed triangle, off-diagonal entries doubled."""
+    Z = np.ascontiguousarray(mol.Z, dtype=np.float64)
+    xyz = np.ascontiguousarray(mol.xyz, dtype=np.float64).reshape(-1)
+    rc = prim.L.gdfjk_potential_grad_device(prim.h, ctypes.c_void_p(Dp_ptr), int(mol.natom), _p(Z), _p(xyz),
+                                            ctypes.c_void_p(grad_ptr), None if not stream else ctypes.c_void_p(stream))
+    if rc != 0:
+        raise GdfjkError(rc, prim.L.gdfjk_last_error(None).decode())
+
+
 def metric_grad_device(aux: DeviceBasis, G2_ptr: int, ldg: int, natom: int, grad_ptr: int, stream: int | None = None):
     """grad[natom][3] (device, accumulated) += sum G2[P][Q] d(P|Q)/dx (gdfjk_metric_grad_device)."""
     rc = aux.L.gdfjk_metric_grad_device(aux.h, ctypes.c_void_p(G2_ptr), int(ldg), int(natom), ctypes.c_void_p(grad_ptr),
@@ -124,15 +136,19 @@ class DeviceDF:
     ints: Integrals
     timings: dict = field(default_factory=dict)
     rows: np.ndarray | None = None  # the first `keep_rows` rows of B (packed triangle), host copy
+    metric_eig: tuple | None = None  # (eigenvalues, eigenvectors) of the metric on the device, when computed there
 
 
-def metric_power_device(Md, power: float, condition: float):
+def metric_power_device(Md, power: float, condition: float, eig=None):
     """Matrix::power (matrix.cc:2370-2415) of a device matrix, with the host restatement's
     rule (dfhelper.metric_power): eigendecompose (the library's FP64 symmetric eigensolver),
-    drop |lambda| < condition * max|lambda| for negative powers, rebuild V diag(lambda^p) V^T."""
+    drop |lambda| < condition * max|lambda| for negative powers, rebuild V diag(lambda^p) V^T.
+    eig: a list that receives (w, V)."""
     import torch
 
     w, V = torch.linalg.eigh(Md)
+    if eig is not None:
+        eig[:] = [w, V]
     max_a = torch.maximum(w[-1].abs(), w[0].abs())
     a = torch.where(w > 0, w.clamp(min=torch.finfo(w.dtype).tiny) ** power, torch.zeros_like(w))
     if power < 0.0:
@@ -164,8 +180,9 @@ def _metric_and_power(ints, aux_dev, naux, condition, dev, timings, power_on="au
         Md = torch.from_numpy(ints.metric()).to(dev)
     M = Md.cpu().numpy()
     tp = time.perf_counter()
+    eig = []
     if power_on == "device":
-        Jm = metric_power_device(Md, -0.5, condition)
+        Jm = metric_power_device(Md, -0.5, condition, eig=eig)
         Jm_host = Jm.cpu().numpy()
         timings.update({"metric_s": tp - tm, "metric_power_device_s": time.perf_counter() - tp})
     else:
@@ -173,6 +190,7 @@ def _metric_and_power(ints, aux_dev, naux, condition, dev, timings, power_on="au
         Jm = torch.from_numpy(Jm_host).to(dev).contiguous()
         timings.update({"metric_s": tp - tm, "metric_power_host_s": time.perf_counter() - tp})
     del Md
+    timings["metric_eig"] = tuple(eig) if eig else None
     return M, Jm_host, Jm
 
 
@@ -253,7 +271,8 @@ def build_device_B(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int 
     del B
     torch.cuda.empty_cache()
     timings["total_s"] = time.perf_counter() - t0
-    return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, rows)
+    eig = timings.pop("metric_eig", None)
+    return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, rows, eig)
 
 
 def build_device_B_screened(mol: Molecule, primary: BasisSet, aux: BasisSet, device: int = 0,
@@ -332,7 +351,8 @@ def build_device_B_screened(mol: Molecule, primary: BasisSet, aux: BasisSet, dev
     t_up = time.perf_counter() - tu
     timings.update({"metric_contraction_device_s": t_gemm, "expand_and_upload_s": t_up, "significant_pairs": int(nsig),
                     "pairs": int(npair), "total_s": time.perf_counter() - t0})
-    return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, None)
+    eig = timings.pop("metric_eig", None)
+    return DeviceDF(eng, nbf, naux, sp, M, Jm_host, ints, timings, None, eig)
 
 
 def slice_pqq(rows: np.ndarray, sp: Sparsity) -> tuple[np.ndarray, Sparsity]:

@@ -38,12 +38,13 @@ def metric_power_frechet(M, W, power=-0.5, condition=1e-10):
     return V @ (Lm * (V.T @ Ws @ V)) @ V.T
 
 
-def metric_power_frechet_device(Md, Wd, power=-0.5, condition=1e-10):
+def metric_power_frechet_device(Md, Wd, power=-0.5, condition=1e-10, eig=None):
     """metric_power_frechet on device arrays (the library's FP64 eigensolver and GEMMs), for
-    large fitting sets; same truncation and divided differences."""
+    large fitting sets; same truncation and divided differences.  eig: the metric's (w, V)
+    from its power at initialisation (the eigensolver is then skipped)."""
     import torch
 
-    w, V = torch.linalg.eigh(Md)
+    w, V = eig if eig is not None else torch.linalg.eigh(Md)
     max_a = torch.maximum(w[-1].abs(), w[0].abs())
     aw = w.abs()
     keep = aw >= condition * max_a if power < 0 else torch.ones_like(w, dtype=torch.bool)
@@ -57,7 +58,8 @@ def metric_power_frechet_device(Md, Wd, power=-0.5, condition=1e-10):
     return V @ (Lm * (V.T @ Ws @ V)) @ V.T
 
 
-def two_electron_gradient_screened(engine, ints, sp, metric, Jmhalf, C, timings=None, batch_q=0, callback=None):
+def two_electron_gradient_screened(engine, ints, sp, metric, Jmhalf, C, timings=None, batch_q=0, callback=None,
+                                   metric_eig=None):
     """The two-electron gradient with every naux x pairs array kept over the significant pairs
     only (the layout of device_init.build_device_B_screened), for systems whose dense triangle
     would not fit (C100H202): Gamma = dE/dB from the engine's batched backward with (Q|mi)
@@ -66,7 +68,8 @@ def two_electron_gradient_screened(engine, ints, sp, metric, Jmhalf, C, timings=
     5e-8 Eh/bohr), A from the integral kernels, the Frechet derivative of M^-1/2 on the device,
     and the derivative contractions in the derivative kernels.  C: occupied orbitals (host);
     the tensor-core forms' copies of B are released first (rebuilt by the next build).
-    callback() is called after each large piece (memory sampling)."""
+    callback() is called after each large piece (memory sampling); metric_eig: the metric's
+    eigenpairs on the device from its power at initialisation (DeviceDF.metric_eig)."""
     import time
 
     import torch
@@ -107,13 +110,18 @@ def two_electron_gradient_screened(engine, ints, sp, metric, Jmhalf, C, timings=
     if callback:
         callback()
     t3 = time.perf_counter()
+    # W = Gamma A^T over chunks of the pairs (the digit copies of both operands stay ~8 GB)
     W = torch.empty((naux, naux), dtype=torch.float64, device=dev)
-    engine.gemm(G.data_ptr(), nsig, A.data_ptr(), nsig, W.data_ptr(), naux, naux, naux, nsig, transb=True)
+    kc = max(1024, int(8e9 / (16.0 * naux)) // 1024 * 1024)
+    for k0 in range(0, nsig, kc):
+        k1 = min(nsig, k0 + kc)
+        engine.gemm(G.data_ptr() + 8 * k0, nsig, A.data_ptr() + 8 * k0, nsig, W.data_ptr(), naux, naux, naux, k1 - k0,
+                    transb=True, accumulate=k0 > 0)
     del A, G
     torch.cuda.empty_cache()
     t4 = time.perf_counter()
     Md = torch.from_numpy(np.ascontiguousarray(metric)).to(dev)
-    G2 = metric_power_frechet_device(Md, W)
+    G2 = metric_power_frechet_device(Md, W, eig=metric_eig)
     del Md, W
     torch.cuda.synchronize(dev)
     t5 = time.perf_counter()
@@ -249,6 +257,34 @@ def one_electron_gradient(mol, ints, scf):
     g += 2.0 * ints.potential_grad(D)
     g -= 2.0 * ints.overlap_grad(W)
     return g
+
+
+def one_electron_gradient_device(mol, ints, scf, device=0):
+    """one_electron_gradient with the nuclear-attraction derivatives on the device
+    (gdfjk_potential_grad_device; O(natom nbf^2) integrals, the expensive part at C100H202);
+    the kinetic and overlap derivatives and E_nuc stay on the host."""
+    import torch
+
+    from .device_init import DeviceBasis, potential_grad_device
+
+    nocc = scf.nocc
+    C = scf.C[:, :nocc]
+    eps = scf.eps[:nocc]
+    D = C @ C.T
+    W = (C * eps) @ C.T
+    g = mol.nuclear_repulsion_grad()
+    g += 2.0 * ints.kinetic_grad(D)
+    g -= 2.0 * ints.overlap_grad(W)
+    nbf = D.shape[0]
+    r, c = np.tril_indices(nbf)
+    Dp = np.where(r == c, 1.0, 2.0) * D[r, c]  # sum over m >= n with both (mn) and (nm)
+    dev = torch.device("cuda", device)
+    Dd = torch.from_numpy(np.ascontiguousarray(Dp)).to(dev)
+    gd = torch.zeros((mol.natom, 3), dtype=torch.float64, device=dev)
+    pd = DeviceBasis(ints.primary, device)
+    potential_grad_device(pd, Dd.data_ptr(), mol, gd.data_ptr())
+    pd.close()
+    return g + 2.0 * gd.cpu().numpy()
 
 
 def rhf_gradient(mol, ints, df, scf, Gamma, engine=None, timings=None):
