@@ -884,12 +884,25 @@ def measure_scf_device_B(cfg, dev):
                             "seconds": time.perf_counter() - ts, "jk_seconds": r_em.timings["jk_s"]}
     jk.reset_incremental()
     sched = PrecisionSchedule(fp64_precision="fp64-emulated")
+    increments = []
+
+    def sample_and_record(*a):
+        sample_memory()
+        inc = getattr(jk, "last_increment_s", None)
+        if inc is not None:
+            increments.append(inc)
+            jk.last_increment_s = None
+
     ts = time.perf_counter()
-    r_pf = rhf(jk, H, S, nocc, e_nuc, schedule=sched, record_orbitals=True, callback=sample_memory,
+    r_pf = rhf(jk, H, S, nocc, e_nuc, schedule=sched, record_orbitals=True, callback=sample_and_record,
                guess_density_factor=Cs)
     out["precision_form"] = {"energy": r_pf.energy, "iterations": r_pf.iterations, "mixed_builds": sched.n_mixed,
                              "fp64_builds": sched.n_fp64, "seconds": time.perf_counter() - ts,
                              "jk_seconds": r_pf.timings["jk_s"]}
+    if increments:
+        out["precision_form"]["increment_mean_s"] = {
+            k: float(np.mean([i[k] for i in increments])) for k in increments[0]}
+        out["precision_form"]["increments"] = len(increments)
     jk.set_incremental(False)
     jk.set_precision("fp64-emulated")
     errs = energy_errors_vs_fp64(r_pf, jk, H, e_nuc)

@@ -151,3 +151,4 @@ def test_incremental_device_entry_matches_host_entry(ints_built, jk_built):
     assert np.array_equal(Jd.cpu().numpy(), Jh) and np.array_equal(Kd.cpu().numpy(), Kh)
     host.close()
     dev.close()
+
