@@ -144,25 +144,6 @@ def two_electron_gradient_screened(engine, ints, sp, metric, Jmhalf, C, timings=
     return out
 
 
-def _metric_products_device(engine, Jmhalf, Gamma, A_raw):
-    """G3 = M^-1/2 Gamma on the tensor cores to FP64 accuracy (gdfjk_gemm_device, the metric
-    contraction's digit product) and W = Gamma A^T as a plain FP64 library product on the same
-    device.  W goes on into the Frechet derivative of M^-1/2, which multiplies errors by up to
-    lambda_min^-3/2 of the kept metric eigenvalues: the digit product's error, relative to the
-    row and column maxima of a run of 1024 pairs, grew to 5e-8 Eh/bohr in the gradient there,
-    so W keeps FP64 rounding.  torch carries the device buffers (and calls the library GEMM)."""
-    import torch
-
-    dev = torch.device("cuda", engine.device)
-    naux, npair = Gamma.shape
-    Gd = torch.from_numpy(np.ascontiguousarray(Gamma)).to(dev)
-    Jm = torch.from_numpy(np.ascontiguousarray(Jmhalf)).to(dev)
-    G3 = torch.empty_like(Gd)
-    engine.gemm(Jm.data_ptr(), naux, Gd.data_ptr(), npair, G3.data_ptr(), npair, naux, npair, naux)
-    W = Gd @ torch.from_numpy(np.ascontiguousarray(A_raw)).to(dev).T
-    return G3.cpu().numpy(), W.cpu().numpy()
-
-
 def _two_electron_gradient_device(engine, ints, df, Gamma, timings):
     """The device path: A = (P|mn) from the integral kernels (screened function pairs zero, as
     in the DF tensor), G3 = M^-1/2 Gamma on the tensor cores, W = Gamma A^T in FP64, the
@@ -218,7 +199,7 @@ def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None
     piece."""
     import time
 
-    if engine is not None and A_raw is None:
+    if engine is not None:
         return _two_electron_gradient_device(engine, ints, df, Gamma, timings)
     t = time.perf_counter()
     if A_raw is None:
@@ -226,11 +207,8 @@ def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None
         r, c = np.tril_indices(df.nbf)
         A_raw[:, ~df.sparsity.pair_mask[r, c]] = 0.0
     t1 = time.perf_counter()
-    if engine is not None:
-        G3, W = _metric_products_device(engine, df.Jmhalf, Gamma, A_raw)
-    else:
-        G3 = df.Jmhalf @ Gamma
-        W = Gamma @ A_raw.T
+    G3 = df.Jmhalf @ Gamma
+    W = Gamma @ A_raw.T
     t2 = time.perf_counter()
     G2 = metric_power_frechet(df.metric, W)
     t3 = time.perf_counter()
@@ -241,7 +219,7 @@ def two_electron_gradient(ints, df, Gamma, A_raw=None, engine=None, timings=None
     if timings is not None:
         timings.update({"three_index_s": t1 - t, "metric_products_s": t2 - t1, "metric_frechet_s": t3 - t2,
                         "three_index_derivative_contraction_s": t4 - t3, "metric_derivative_contraction_s": t5 - t4,
-                        "metric_products_on": "tensor cores" if engine is not None else "host"})
+                        "metric_products_on": "host"})
     return g3 + g2
 
 
@@ -289,15 +267,7 @@ def one_electron_gradient_device(mol, ints, scf, device=0):
 
 def rhf_gradient(mol, ints, df, scf, Gamma, engine=None, timings=None):
     """Total RHF gradient (natom x 3, Eh/bohr) from a converged SCF and the engine's Gamma
-    for gJ = dE/dJ = 2D, gK = dE/dK = -D (the metric products on `engine` when given)."""
-    nocc = scf.nocc
-    C = scf.C[:, :nocc]
-    eps = scf.eps[:nocc]
-    D = C @ C.T
-    W = (C * eps) @ C.T
-    g = mol.nuclear_repulsion_grad()
-    g += 2.0 * ints.kinetic_grad(D)
-    g += 2.0 * ints.potential_grad(D)
-    g -= 2.0 * ints.overlap_grad(W)
-    g += two_electron_gradient(ints, df, Gamma, engine=engine, timings=timings)
-    return g
+    for gJ = dE/dJ = 2D, gK = dE/dK = -D: with `engine` the two-electron part on its device,
+    else on the host (the one-electron terms on the host either way)."""
+    return one_electron_gradient(mol, ints, scf) + two_electron_gradient(ints, df, Gamma, engine=engine,
+                                                                         timings=timings)
