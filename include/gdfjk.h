@@ -226,7 +226,8 @@ int gdfjk_compute_incremental_device(gdfjk_t h, const double* C, int nocc, int l
 /* Gamma = dE/dB of gdfjk_backward alone, for systems whose full-size backward workspaces do
  * not fit (the C100H202 gradient): device C, gJ, gK; the aux functions are taken in batches of
  * batch_q (0: as many as fit GDFJK_BW_BATCH_GB, default 16 GB, of X_b and Y_b), X_b = B_b C
- * recomputed per batch ((Q|mi) never stored whole), Y_b = gK X_b on the tensor cores to FP64
+ * recomputed per batch ((Q|mi) never stored whole), Y_b = gK X_b and Y_Q C^T (the dense part of
+ * Gamma, GDFJK_BW_GAMMA_GB, default 8 GB, of it at a time) on the tensor cores to FP64
  * accuracy (the digit product of gdfjk_gemm_device), and Gamma written into the device array
  * Gamma (naux rows, leading dimension ldg; packed-triangle columns, or col_map[m(m+1)/2+n],
  * < 0 = not stored; cleared first).  Returns when complete. */

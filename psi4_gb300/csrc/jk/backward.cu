@@ -148,6 +148,55 @@ void launch_gamma(const double* Y, const double* C, const double* gJ, const doub
                                            col_map);
 }
 
+// Y (layout [m][Q][i], nq aux functions) -> Yq[Q'][m][i] for Q = qs0 + Q', Q' < nqs
+__global__ void y_to_qmajor_kernel(const double* __restrict__ Y, int nq, int qs0, int nqs, int nbf_pad, int nocc_pad,
+                                   double* __restrict__ Yq) {
+    const size_t n = (size_t)nqs * nbf_pad * nocc_pad;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % nocc_pad);
+        const size_t r = e / nocc_pad;
+        const int m = (int)(r % nbf_pad), q = (int)(r / nbf_pad);
+        Yq[e] = Y[((size_t)m * nq + qs0 + q) * nocc_pad + i];
+    }
+}
+
+void launch_y_to_qmajor(const double* Y, int nq, int qs0, int nqs, int nbf_pad, int nocc_pad, double* Yq,
+                        cudaStream_t stream) {
+    const size_t n = (size_t)nqs * nbf_pad * nocc_pad;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    y_to_qmajor_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(Y, nq, qs0, nqs, nbf_pad, nocc_pad, Yq);
+}
+
+// Gamma from P[Q][m][n] = sum_i Y_Q[m][i] C[n][i] (a dense product): for each listed pair
+// (m >= n, column col) out[Q*ldo + col] = (2 if m > n) (P[m][n] + P[n][m] + gJ_mn d_Q + g_Q D_mn),
+// the same value gamma_kernel forms from Y and C directly.
+__global__ void gamma_gather_kernel(const double* __restrict__ P, int nqs, int nbf_pad, const int* __restrict__ pm,
+                                    const int* __restrict__ pn, const int* __restrict__ pcol, size_t npairs,
+                                    const double* __restrict__ gJ, const double* __restrict__ D,
+                                    const double* __restrict__ dq, const double* __restrict__ gq,
+                                    double* __restrict__ out, size_t ldo) {
+    const size_t n = npairs * nqs;
+    const size_t np2 = (size_t)nbf_pad * nbf_pad;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int q = (int)(e / npairs);
+        const size_t k = e % npairs;
+        const size_t m = (size_t)pm[k], nn = (size_t)pn[k];
+        const double* PQ = P + (size_t)q * np2;
+        const size_t mn = m * nbf_pad + nn;
+        const double v = PQ[mn] + PQ[nn * nbf_pad + m] + gJ[mn] * dq[q] + gq[q] * D[mn];
+        out[(size_t)q * ldo + (size_t)pcol[k]] = (m > nn ? 2.0 : 1.0) * v;
+    }
+}
+
+void launch_gamma_gather(const double* P, int nqs, int nbf_pad, const int* pm, const int* pn, const int* pcol,
+                         size_t npairs, const double* gJ, const double* D, const double* dq, const double* gq,
+                         double* out, size_t ldo, cudaStream_t stream) {
+    const size_t n = npairs * nqs;
+    if (n == 0) return;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+    gamma_gather_kernel<<<blocks, 256, 0, stream>>>(P, nqs, nbf_pad, pm, pn, pcol, npairs, gJ, D, dq, gq, out, ldo);
+}
+
 // out[e] = alpha * sum_{b < nblk} part[b*n + e] + beta * out[e]   (fixed order)
 __global__ void reduce_blocks_kernel(const double* __restrict__ part, int nblk, size_t n, double alpha, double beta,
                                      double* __restrict__ out) {

@@ -132,6 +132,12 @@ void launch_gemm_nn_fp64(int M, size_t N, int K, const double* A, size_t lda, co
 void launch_gamma(const double* Y, const double* C, const double* gJ, const double* D, const double* dq,
                   const double* gq, int naux, int nbf, int nbf_pad, int nocc_pad, const TileLayout& L, double* out,
                   cudaStream_t stream, size_t ldo = 0, const long long* col_map = nullptr);
+// the batched backward's tensor-core Gamma: Y to Q-major rows, then the listed pairs of P
+void launch_y_to_qmajor(const double* Y, int nq, int qs0, int nqs, int nbf_pad, int nocc_pad, double* Yq,
+                        cudaStream_t stream);
+void launch_gamma_gather(const double* P, int nqs, int nbf_pad, const int* pm, const int* pn, const int* pcol,
+                         size_t npairs, const double* gJ, const double* D, const double* dq, const double* gq,
+                         double* out, size_t ldo, cudaStream_t stream);
 void launch_reduce_blocks(const double* part, int nblk, size_t n, double alpha, double beta, double* out,
                           cudaStream_t stream);
 void launch_copy_rect(const double* src, int nbf, int nocc, int nocc_pad, double* dst, int ldd, cudaStream_t stream);

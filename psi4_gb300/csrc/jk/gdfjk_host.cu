@@ -1009,16 +1009,62 @@ int gdfjk_backward_gamma_device(gdfjk_t h, const double* C, int nocc, int ldc, c
         qb = (int)std::max(1.0, std::floor(gb * 1e9 / per_q));
     }
     qb = std::max(1, std::min({qb, naux, 65535}));
-    double *Xb = nullptr, *Yb = nullptr;
+    // Gamma_Q = Y_Q C^T + C Y_Q^T (+ the Coulomb terms) as P = Y_Q C^T on the tensor cores for
+    // sub-batches of qs aux functions (P within GDFJK_BW_GAMMA_GB, default 8 GB), then a gather
+    // of the listed pairs: those of the stored tiles (m >= n) that Gamma keeps
+    int qs;
+    {
+        const char* e = getenv("GDFJK_BW_GAMMA_GB");
+        double gb = e ? atof(e) : 8.0;
+        if (!(gb > 0.0)) gb = 8.0;
+        qs = (int)std::max(1.0, std::floor(gb * 1e9 / ((double)nbf_pad * nbf_pad * 8.0)));
+        qs = std::min(qs, qb);
+    }
+    std::vector<int> pm, pn, pcol;
+    {
+        std::vector<int64_t> cm;
+        if (col_map) {
+            cm.resize(npair);
+            CK(cudaMemcpy(cm.data(), col_map, npair * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        }
+        for (int t = 0; t < h->ntiles; ++t) {
+            const int I = h->tI[t], J = h->tJ[t];
+            for (int r = 0; r < TILE; ++r)
+                for (int c = 0; c < TILE; ++c) {
+                    const int m = I * TILE + r, n = J * TILE + c;
+                    if (m >= nbf || n >= nbf || m < n) continue;
+                    const size_t tri = (size_t)m * (m + 1) / 2 + n;
+                    const int64_t col = col_map ? cm[tri] : (int64_t)tri;
+                    if (col < 0) continue;
+                    pm.push_back(m);
+                    pn.push_back(n);
+                    pcol.push_back((int)col);
+                }
+        }
+    }
+    double *Xb = nullptr, *Yb = nullptr, *Yq = nullptr, *Pq = nullptr;
+    int *d_pm = nullptr, *d_pn = nullptr, *d_pcol = nullptr;
     auto release = [&]() {
-        if (Xb) cudaFree(Xb);
-        if (Yb) cudaFree(Yb);
-        Xb = Yb = nullptr;
+        void* ps[] = {Xb, Yb, Yq, Pq, d_pm, d_pn, d_pcol};
+        for (void* p : ps)
+            if (p) cudaFree(p);
+        Xb = Yb = Yq = Pq = nullptr;
+        d_pm = d_pn = d_pcol = nullptr;
     };
     const size_t be = (size_t)nbf_pad * qb * nocc_pad;
-    if ((rc = dalloc(h, &Xb, be)) || (rc = dalloc(h, &Yb, be))) {
+    const size_t npl = pm.size();
+    if ((rc = dalloc(h, &Xb, be)) || (rc = dalloc(h, &Yb, be)) ||
+        (rc = dalloc(h, &Yq, (size_t)qs * nbf_pad * nocc_pad)) || (rc = dalloc(h, &Pq, (size_t)qs * nbf_pad * nbf_pad)) ||
+        (rc = dalloc(h, &d_pm, std::max<size_t>(npl, 1))) || (rc = dalloc(h, &d_pn, std::max<size_t>(npl, 1))) ||
+        (rc = dalloc(h, &d_pcol, std::max<size_t>(npl, 1)))) {
         release();
         return rc;
+    }
+    if (npl > 0 && (cudaMemcpy(d_pm, pm.data(), npl * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+                    cudaMemcpy(d_pn, pn.data(), npl * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+                    cudaMemcpy(d_pcol, pcol.data(), npl * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)) {
+        release();
+        return set_err(h, GDFJK_ERR_CUDA, "backward_gamma: copy of the pair list failed");
     }
     TileLayout L = layout_of(h);
     launch_pad_C(C, nbf, nocc, ldc, nbf_pad, nocc_pad, h->Cl, s);
@@ -1045,8 +1091,18 @@ int gdfjk_backward_gamma_device(gdfjk_t h, const double* C, int nocc, int ldc, c
             release();
             return set_err(h, rc, "backward_gamma: " + h->err);
         }
-        launch_gamma(Yb, h->Cl, h->gJp, h->D, h->dq + q0, h->gq + q0, nq, nbf, nbf_pad, nocc_pad, L,
-                     Gamma + (size_t)q0 * ldg, s, (size_t)ldg, reinterpret_cast<const long long*>(col_map));
+        for (int qs0 = 0; qs0 < nq; qs0 += qs) {
+            const int nqs = std::min(qs, nq - qs0);
+            launch_y_to_qmajor(Yb, nq, qs0, nqs, nbf_pad, nocc_pad, Yq, s);
+            rc = oz_gemm(h->oz, Yq, (size_t)nocc_pad, h->Cl, (size_t)nocc_pad, Pq, (size_t)nbf_pad, nqs * nbf_pad, nbf_pad,
+                         nocc_pad, 0, s, h->err, 1);
+            if (rc) {
+                release();
+                return set_err(h, rc, "backward_gamma: " + h->err);
+            }
+            launch_gamma_gather(Pq, nqs, nbf_pad, d_pm, d_pn, d_pcol, npl, h->gJp, h->D, h->dq + q0 + qs0,
+                                h->gq + q0 + qs0, Gamma + (size_t)(q0 + qs0) * ldg, (size_t)ldg, s);
+        }
     }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -243,37 +243,22 @@ def _timed_factor(C_new, C_old):
 def density_difference_factor(C_new, C_old, tol=1e-13):
     """Signed low-rank factor of dD = C_new C_new^T - C_old C_old^T.
 
-    QR of [C_new, C_old] = Q R gives dD = Q (R S R^T) Q^T with S = diag(+1.., -1..).  The small
-    symmetric indefinite M = R S R^T is factored as P L D L^T P^T (Bunch-Kaufman, LAPACK's
-    dsytrf through scipy.linalg.ldl: D block diagonal with 1x1 and 2x2 blocks, L bounded), each
-    2x2 block of D diagonalised in closed form, so dD = U+ U+^T - U- U-^T with
-    U = Q L V |lam|^1/2, positive terms first: |U|^2 ~ |dD| as with an eigendecomposition of M,
-    at a fraction of its cost (the factor has to be ready when the GPU's J is).  Terms with
-    |lam| <= tol are dropped.  Returns (U, npos)."""
-    from scipy.linalg import ldl
-
+    QR of [C_new, C_old] = Q R gives dD = Q (R S R^T) Q^T with S = diag(+1.., -1..); the small
+    symmetric R S R^T = W diag(lam) W^T then gives dD = U+ U+^T - U- U-^T with
+    U = Q W |lam|^1/2, positive eigenvalues first: orthogonal columns of norm |lam|^1/2, so the
+    split-precision increment's rounding scales with dD itself (a triangular LDL^T factor of
+    R S R^T was tried: cheaper, but its non-orthogonal columns cancel, and at C100H202 the SCF
+    then needed two more FP64 builds).  Eigenvalues below `tol` are dropped.
+    Returns (U, npos)."""
     A = np.hstack([C_new, C_old])
     Q, R = np.linalg.qr(A)
     sgn = np.concatenate([np.ones(C_new.shape[1]), -np.ones(C_old.shape[1])])
-    M = (R * sgn) @ R.T
-    Lf, Dm, _ = ldl(0.5 * (M + M.T), lower=True, hermitian=True)
-    n = Dm.shape[0]
-    lam = np.empty(n)
-    i = 0
-    while i < n:
-        if i + 1 < n and Dm[i + 1, i] != 0.0:  # a 2x2 pivot: rotate its two columns of L
-            w, v = np.linalg.eigh(Dm[i:i + 2, i:i + 2])
-            Lf[:, i:i + 2] = Lf[:, i:i + 2] @ v
-            lam[i:i + 2] = w
-            i += 2
-        else:
-            lam[i] = Dm[i, i]
-            i += 1
+    lam, W = np.linalg.eigh((R * sgn) @ R.T)
     keep = np.abs(lam) > tol
-    lam, Lf = lam[keep], Lf[:, keep]
-    order = np.argsort(-lam, kind="stable")
-    lam, Lf = lam[order], Lf[:, order]
-    U = (Q @ Lf) * np.sqrt(np.abs(lam))
+    lam, W = lam[keep], W[:, keep]
+    order = np.argsort(-lam)
+    lam, W = lam[order], W[:, order]
+    U = (Q @ W) * np.sqrt(np.abs(lam))
     return np.ascontiguousarray(U), int((lam > 0).sum())
 
 
