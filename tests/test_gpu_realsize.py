@@ -1,10 +1,10 @@
 """Parity at the full configurations on real integrals: (H2O)_32 cc-pVTZ (nbf 1856, naux 4448,
 nocc 160) and (H2O)_64 cc-pVDZ (nbf 1536, naux 7424, nocc 320).
 
-B = J^-1/2 (P|mn) is built on the device from the host integrals (psi4_gb300.device_init),
-exactly as the SCF workloads build it.  Orbitals are physical: the core guess and an
-iterate four SCF iterations in.  Bars, all absolute (the benchmark spec: J and K to 1e-10 in max
-absolute element against FP64):
+B = J^-1/2 (P|mn) is built on the device from the engine's integral kernels
+(psi4_gb300.device_init), exactly as the SCF workloads build it.  Orbitals are physical: the
+core guess and an iterate four SCF iterations in.  Bars, all absolute (the parity bar: J and K
+to 1e-10 in max absolute element against FP64):
 
 * emulated-FP64 J/K against native FP64 J/K of the same engine: 1e-10;
 * native FP64 J/K against the oracle's loop restatement of DFHelper (compute_J_symm /
