@@ -100,6 +100,11 @@ struct gdfjk_s {
     int flags = 0;
     std::vector<int> tI, tJ, map;
     cudaStream_t stream = nullptr;
+    // J runs on its own stream, forked after D and joined before the build ends, so that its
+    // FP64 / HBM-bound passes overlap the tensor-core K kernels on `stream`
+    cudaStream_t stream_j = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool j_pending = false;
     int *d_tI = nullptr, *d_tJ = nullptr, *d_map = nullptr;
     int* d_err = nullptr;  // device-side error flag word
     double* B = nullptr;   // naux * ntiles * 4096
@@ -233,8 +238,21 @@ int ensure_workspace(gdfjk_t h, int nocc_pad, bool nonsym, bool need_x) {
 namespace {
 
 // Enqueue one build on the handle's stream; all pointers are device pointers.
+// J (when asked) goes to h->stream_j after D, so that its two HBM-bound passes over B fill the
+// SMs the tensor-core K kernels leave idle (the tail waves of the half-transform, the
+// contraction, the reductions).  The native FP64 K, FP64-pipe work like J, runs after J on the
+// one stream.  J joins h->stream at the end (join = false leaves the join to the caller: join_j).
+constexpr double J_FORK_MIN_BYTES = 8e9;  // B of at least this size: J on the second stream
+
+void join_j(gdfjk_t h) {
+    if (h->j_pending) {
+        cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+        h->j_pending = false;
+    }
+}
+
 int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode, double* D_out,
-                  double* J, double* K) {
+                  double* J, double* K, bool join = true) {
     const bool do_J = mode & GDFJK_DO_J;
     const bool do_K = mode & GDFJK_DO_K;
     const bool nonsym = C_right != nullptr;
@@ -260,19 +278,39 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
     launch_density(h->Cl, nonsym ? h->Cr : h->Cl, h->nbf_pad, nocc_pad, h->D, s);
     if (D_out) launch_copy_out(h->D, h->nbf, h->nbf_pad, D_out, s);
     if (do_J) {
-        launch_weighted_density_tiles(h->D, h->nbf_pad, L, h->Dw, s);
-        launch_j_pass1(h->B, h->Dw, h->naux, L, h->dq, s);
-        launch_j_pass2(h->B, h->dq, h->naux, L, h->Jt, s);
-        launch_unpack_tiles(h->Jt, L, h->nbf, h->nbf_pad, J, h->nbf, true, s);
+        // J on the second stream only beside a tensor-core K (or alone, when the caller joins
+        // later) and only on a large B.  Measured on one GB300: at nbf 1856 / naux 4448 (61 GB
+        // of B) the emulated build went from 224 to 215 ms; at nbf 384 / naux 1856 (1.3 GB,
+        // J well under a millisecond) it went from 4.7 to 5.0 ms
+        const bool tc_k = !do_K || (mode & (GDFJK_MIXED | GDFJK_EMULATED));
+        const bool fork = tc_k && (double)h->naux * h->ntiles * 4096 * sizeof(double) >= J_FORK_MIN_BYTES;
+        cudaStream_t sj = fork ? h->stream_j : s;
+        if (fork) {
+            CK(cudaEventRecord(h->ev_fork, s));
+            CK(cudaStreamWaitEvent(sj, h->ev_fork, 0));
+        }
+        launch_weighted_density_tiles(h->D, h->nbf_pad, L, h->Dw, sj);
+        launch_j_pass1(h->B, h->Dw, h->naux, L, h->dq, sj);
+        launch_j_pass2(h->B, h->dq, h->naux, L, h->Jt, sj);
+        launch_unpack_tiles(h->Jt, L, h->nbf, h->nbf_pad, J, h->nbf, true, sj);
+        CK(cudaEventRecord(h->ev[1], sj));
+        if (fork) {
+            CK(cudaEventRecord(h->ev_join, sj));
+            h->j_pending = true;
+        }
+    } else {
+        CK(cudaEventRecord(h->ev[1], s));
     }
-    CK(cudaEventRecord(h->ev[1], s));
     CK(cudaEventRecord(h->ev[2], s));
     if (do_K) {
         if (nocc == 0) {
             CK(cudaMemsetAsync(K, 0, sizeof(double) * (size_t)h->nbf * h->nbf, s));
             CK(cudaEventRecord(h->ev[3], s));
         } else if (mode & GDFJK_MIXED) {
-            if (nonsym) return set_err(h, GDFJK_ERR_ARG, "mixed-precision K needs an lr-symmetric density");
+            if (nonsym) {
+                join_j(h);
+                return set_err(h, GDFJK_ERR_ARG, "mixed-precision K needs an lr-symmetric density");
+            }
             rc = mixed_build_K(h->mixed, h->B, L, h->map.data(), h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
                                h->ev[3], s, h->err);
             if (rc == GDFJK_ERR_OOM) {  // give the emulated form's caches back and retry once
@@ -281,7 +319,10 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
                 rc = mixed_build_K(h->mixed, h->B, L, h->map.data(), h->nbf, h->nbf_pad, h->naux, h->Cl, nocc, nocc_pad, mode, K,
                                    h->ev[3], s, h->err);
             }
-            if (rc) return rc;
+            if (rc) {
+                join_j(h);
+                return rc;
+            }
         } else if (mode & GDFJK_EMULATED) {
             h->last_emulated = true;
             const double* Cr = nonsym ? h->Cr : nullptr;
@@ -293,7 +334,10 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
                 rc = oz_build_K(h->oz, h->B, L, h->map.data(), h->nbf, h->naux, h->Cl, Cr, nocc, nocc_pad, K, h->ev[3], s,
                                 h->err);
             }
-            if (rc) return rc;
+            if (rc) {
+                join_j(h);
+                return rc;
+            }
         } else {
             launch_k_transform_fp64(h->B, h->Cl, h->naux, h->nbf_pad, nocc_pad, L, h->Xl, s);
             if (nonsym) launch_k_transform_fp64(h->B, h->Cr, h->naux, h->nbf_pad, nocc_pad, L, h->Xr, s);
@@ -309,6 +353,7 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
     } else {
         CK(cudaEventRecord(h->ev[3], s));
     }
+    if (join) join_j(h);
     CK(cudaEventRecord(h->ev[4], s));
     CK(cudaGetLastError());
     return GDFJK_OK;
@@ -419,7 +464,14 @@ int gdfjk_create(int device, int nbf, int naux, const unsigned char* pair_mask, 
         gdfjk_destroy(h);
         return code;
     };
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // K's stream at the highest priority, J's at the lowest: when an SM frees resources the
+    // block scheduler places K's persistent CTAs first and J's small blocks in what is left
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&h->stream_j, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         h->err = "cudaStreamCreate failed";
         return fail(GDFJK_ERR_CUDA);
     }
@@ -453,6 +505,7 @@ int gdfjk_destroy(gdfjk_t h) {
     if (!h) return GDFJK_OK;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->stream_j) cudaStreamSynchronize(h->stream_j);
     big_free(h->B);
     double* bufs[] = {h->Cl,  h->Cr,  h->D,     h->Dw,  h->dq,  h->Jt,  h->Xl, h->Xr,  h->Kpart,
                       h->Kt,  h->dJ,  h->dK,  h->dD,    h->dCin, h->dCrin, h->gJp, h->gKp, h->Jg, h->Yb,
@@ -467,7 +520,10 @@ int gdfjk_destroy(gdfjk_t h) {
     oz_destroy(h->oz);
     for (auto& ev : h->ev)
         if (ev) cudaEventDestroy(ev);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->stream_j) cudaStreamDestroy(h->stream_j);
     delete h;
     return GDFJK_OK;
 }
@@ -802,9 +858,13 @@ int enqueue_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const dou
     const size_t n2 = (size_t)h->nbf * h->nbf;
     cudaStream_t s = h->stream;
     if (mode & GDFJK_DO_J) {
-        rc = enqueue_build(h, nocc > 0 ? C : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_J, nullptr, J, nullptr);
-        if (rc) return rc;
-        launch_finite_check(J, n2, h->d_err, s);
+        // J on its own stream, joined after K below so that the two overlap
+        rc = enqueue_build(h, nocc > 0 ? C : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_J, nullptr, J, nullptr,
+                           false);
+        if (rc) {
+            join_j(h);
+            return rc;
+        }
     }
     if ((mode & GDFJK_DO_K) && !(mode & GDFJK_MIXED)) {
         // FP64 anchor: a full FP64 K from C that becomes the base of later increments
@@ -829,6 +889,10 @@ int enqueue_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const dou
         if (rc) return rc;
         CK(cudaEventRecord(h->ev[4], s));
         launch_finite_check(K, n2, h->d_err, s);
+    }
+    if (mode & GDFJK_DO_J) {
+        join_j(h);
+        launch_finite_check(J, n2, h->d_err, s);
     }
     CK(cudaGetLastError());
     return GDFJK_OK;

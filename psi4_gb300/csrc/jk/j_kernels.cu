@@ -132,8 +132,10 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 
 // ---------------------------------------------------------------- J pass 1: d_Q
 // One block per Q; the block streams B_Q (ntiles*4096 doubles, contiguous) once with
-// 16-byte loads, four independent partial sums per thread; Dw stays L2 resident.
-constexpr int JP1_THREADS = 512;
+// 16-byte loads, four independent partial sums per thread; Dw stays L2 resident.  Blocks are
+// small (256 threads, no dynamic shared memory) so that they fit beside a tensor-core K
+// kernel's CTA on the same SM: the J passes run on their own stream, concurrently with K.
+constexpr int JP1_THREADS = 256;
 __global__ void __launch_bounds__(JP1_THREADS) j_pass1_kernel(const double* __restrict__ B,
                                                               const double* __restrict__ Dw, size_t per_q,
                                                               double* __restrict__ dq) {
@@ -168,6 +170,12 @@ void launch_j_pass1(const double* B, const double* Dw, int naux, const TileLayou
         cudaMemsetAsync(dq, 0, sizeof(double) * naux, stream);
         return;
     }
+    static bool carveout = [] {  // keep the SM in the K kernels' shared-memory configuration
+        cudaFuncSetAttribute(j_pass1_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        return true;
+    }();
+    (void)carveout;
     j_pass1_kernel<<<naux, JP1_THREADS, 0, stream>>>(B, Dw, per_q, dq);
 }
 
@@ -175,7 +183,7 @@ void launch_j_pass1(const double* B, const double* Dw, int naux, const TileLayou
 // Each block owns 1024 consecutive tile elements (2 double2 per thread) and sweeps all Q,
 // taking d_Q from shared memory in chunks; fixed Q order per element.
 constexpr int JP2_THREADS = 256;
-constexpr int JP2_DCHUNK = 2048;
+constexpr int JP2_DCHUNK = 128;  // 1 KB of d_Q in shared memory: fits beside the K kernels' 224 KB
 __global__ void __launch_bounds__(JP2_THREADS) j_pass2_kernel(const double* __restrict__ B,
                                                               const double* __restrict__ dq, int naux, size_t per_q,
                                                               double* __restrict__ Jt) {
@@ -234,6 +242,12 @@ void launch_j_pass2(const double* B, const double* dq, int naux, const TileLayou
     if (per_q == 0) return;
     size_t n2 = per_q / 2;
     int blocks = (int)((n2 + 2 * JP2_THREADS - 1) / (2 * JP2_THREADS));
+    static bool carveout = [] {
+        cudaFuncSetAttribute(j_pass2_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        return true;
+    }();
+    (void)carveout;
     j_pass2_kernel<<<blocks, JP2_THREADS, 0, stream>>>(B, dq, naux, per_q, Jt);
 }
 
