@@ -180,44 +180,56 @@ void launch_j_pass1(const double* B, const double* Dw, int naux, const TileLayou
 }
 
 // ---------------------------------------------------------------- J pass 2: J tiles
-// Each block owns 1024 consecutive tile elements (2 double2 per thread) and sweeps all Q,
-// taking d_Q from shared memory in chunks; fixed Q order per element.
+// Each block owns 2 * (256 / QG) consecutive double2 of the tile elements and sweeps all Q,
+// taking d_Q from shared memory in chunks.  QG = 1: every thread sums all Q for its elements.
+// QG > 1 (small tile counts, where one block per 1024 elements leaves most SMs idle): the
+// block's threads form QG groups, group g sums the Q of each chunk with q = g (mod QG), and the
+// QG partial sums of an element are added in group order at the end.  Either way each
+// element's Q order is fixed, so builds are bitwise repeatable.
 constexpr int JP2_THREADS = 256;
-constexpr int JP2_DCHUNK = 128;  // 1 KB of d_Q in shared memory: fits beside the K kernels' 224 KB
+// d_Q staged per chunk: 1 KB for QG = 1, which fits beside the K kernels' 224 KB; 8 KB for the
+// split form (small systems, where J does not run beside K), with fewer block barriers
+constexpr int JP2_QG_SMALL = 8;
+constexpr int JP2_MIN_BLOCKS = 304;  // below this many QG = 1 blocks, split Q
+template <int QG>
 __global__ void __launch_bounds__(JP2_THREADS) j_pass2_kernel(const double* __restrict__ B,
                                                               const double* __restrict__ dq, int naux, size_t per_q,
                                                               double* __restrict__ Jt) {
-    __shared__ double ds[JP2_DCHUNK];
-    size_t base2 = (size_t)blockIdx.x * (2 * JP2_THREADS) + threadIdx.x;  // double2 index
+    constexpr int GT = JP2_THREADS / QG;  // threads of a group
+    constexpr int DCHUNK = QG > 1 ? 1024 : 128;
+    __shared__ double ds[DCHUNK];
+    __shared__ double2 red[QG > 1 ? QG * 2 * GT : 1];
+    const int g = threadIdx.x / GT, r = threadIdx.x % GT;
+    size_t base2 = (size_t)blockIdx.x * (2 * GT) + r;  // double2 index
     size_t n2 = per_q / 2;
     const double2* b = reinterpret_cast<const double2*>(B);
     size_t qstride = n2;
-    bool ok0 = base2 < n2, ok1 = base2 + JP2_THREADS < n2;
+    bool ok0 = base2 < n2, ok1 = base2 + GT < n2;
     double2 acc0 = make_double2(0, 0), acc1 = make_double2(0, 0);
-    for (int q0 = 0; q0 < naux; q0 += JP2_DCHUNK) {
-        int nq = min(JP2_DCHUNK, naux - q0);
+    for (int q0 = 0; q0 < naux; q0 += DCHUNK) {
+        int nq = min(DCHUNK, naux - q0);
         __syncthreads();
         for (int k = threadIdx.x; k < nq; k += JP2_THREADS) ds[k] = dq[q0 + k];
         __syncthreads();
-        const double2* bq = b + (size_t)q0 * qstride + base2;
-        int q = 0;
-        for (; q + 3 < nq; q += 4) {
-            double d0 = ds[q], d1 = ds[q + 1], d2 = ds[q + 2], d3 = ds[q + 3];
+        const double2* bq = b + (size_t)(q0 + g) * qstride + base2;
+        int q = g;
+        for (; q + 3 * QG < nq; q += 4 * QG) {
+            double d0 = ds[q], d1 = ds[q + QG], d2 = ds[q + 2 * QG], d3 = ds[q + 3 * QG];
             double2 x0 = ok0 ? __ldcs(bq) : make_double2(0, 0);
-            double2 x1 = ok0 ? __ldcs(bq + qstride) : make_double2(0, 0);
-            double2 x2 = ok0 ? __ldcs(bq + 2 * qstride) : make_double2(0, 0);
-            double2 x3 = ok0 ? __ldcs(bq + 3 * qstride) : make_double2(0, 0);
-            double2 y0 = ok1 ? __ldcs(bq + JP2_THREADS) : make_double2(0, 0);
-            double2 y1 = ok1 ? __ldcs(bq + qstride + JP2_THREADS) : make_double2(0, 0);
-            double2 y2 = ok1 ? __ldcs(bq + 2 * qstride + JP2_THREADS) : make_double2(0, 0);
-            double2 y3 = ok1 ? __ldcs(bq + 3 * qstride + JP2_THREADS) : make_double2(0, 0);
+            double2 x1 = ok0 ? __ldcs(bq + QG * qstride) : make_double2(0, 0);
+            double2 x2 = ok0 ? __ldcs(bq + 2 * QG * qstride) : make_double2(0, 0);
+            double2 x3 = ok0 ? __ldcs(bq + 3 * QG * qstride) : make_double2(0, 0);
+            double2 y0 = ok1 ? __ldcs(bq + GT) : make_double2(0, 0);
+            double2 y1 = ok1 ? __ldcs(bq + QG * qstride + GT) : make_double2(0, 0);
+            double2 y2 = ok1 ? __ldcs(bq + 2 * QG * qstride + GT) : make_double2(0, 0);
+            double2 y3 = ok1 ? __ldcs(bq + 3 * QG * qstride + GT) : make_double2(0, 0);
             acc0.x = fma(d3, x3.x, fma(d2, x2.x, fma(d1, x1.x, fma(d0, x0.x, acc0.x))));
             acc0.y = fma(d3, x3.y, fma(d2, x2.y, fma(d1, x1.y, fma(d0, x0.y, acc0.y))));
             acc1.x = fma(d3, y3.x, fma(d2, y2.x, fma(d1, y1.x, fma(d0, y0.x, acc1.x))));
             acc1.y = fma(d3, y3.y, fma(d2, y2.y, fma(d1, y1.y, fma(d0, y0.y, acc1.y))));
-            bq += 4 * qstride;
+            bq += 4 * QG * qstride;
         }
-        for (; q < nq; ++q) {
+        for (; q < nq; q += QG) {
             double d0 = ds[q];
             if (ok0) {
                 double2 x0 = __ldcs(bq);
@@ -225,30 +237,55 @@ __global__ void __launch_bounds__(JP2_THREADS) j_pass2_kernel(const double* __re
                 acc0.y = fma(d0, x0.y, acc0.y);
             }
             if (ok1) {
-                double2 y0 = __ldcs(bq + JP2_THREADS);
+                double2 y0 = __ldcs(bq + GT);
                 acc1.x = fma(d0, y0.x, acc1.x);
                 acc1.y = fma(d0, y0.y, acc1.y);
             }
-            bq += qstride;
+            bq += QG * qstride;
+        }
+    }
+    if (QG > 1) {
+        red[g * 2 * GT + r] = acc0;
+        red[g * 2 * GT + GT + r] = acc1;
+        __syncthreads();
+        if (g != 0) return;
+        acc0 = red[r];
+        acc1 = red[GT + r];
+#pragma unroll
+        for (int k = 1; k < QG; ++k) {
+            const double2 u = red[k * 2 * GT + r], v = red[k * 2 * GT + GT + r];
+            acc0.x += u.x;
+            acc0.y += u.y;
+            acc1.x += v.x;
+            acc1.y += v.y;
         }
     }
     double2* out = reinterpret_cast<double2*>(Jt);
     if (ok0) out[base2] = acc0;
-    if (ok1) out[base2 + JP2_THREADS] = acc1;
+    if (ok1) out[base2 + GT] = acc1;
 }
 
 void launch_j_pass2(const double* B, const double* dq, int naux, const TileLayout& L, double* Jt, cudaStream_t stream) {
     size_t per_q = (size_t)L.ntiles * TILE_ELEMS;
     if (per_q == 0) return;
     size_t n2 = per_q / 2;
-    int blocks = (int)((n2 + 2 * JP2_THREADS - 1) / (2 * JP2_THREADS));
     static bool carveout = [] {
-        cudaFuncSetAttribute(j_pass2_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+        cudaFuncSetAttribute(j_pass2_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(j_pass2_kernel<JP2_QG_SMALL>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
         return true;
     }();
     (void)carveout;
-    j_pass2_kernel<<<blocks, JP2_THREADS, 0, stream>>>(B, dq, naux, per_q, Jt);
+    // the choice depends on the sizes only, so a given system always sums in the same order
+    const size_t blocks1 = (n2 + 2 * JP2_THREADS - 1) / (2 * JP2_THREADS);
+    if (blocks1 >= (size_t)JP2_MIN_BLOCKS) {
+        j_pass2_kernel<1><<<(unsigned)blocks1, JP2_THREADS, 0, stream>>>(B, dq, naux, per_q, Jt);
+    } else {
+        constexpr int GT = JP2_THREADS / JP2_QG_SMALL;
+        const size_t blocks = (n2 + 2 * GT - 1) / (2 * GT);
+        j_pass2_kernel<JP2_QG_SMALL><<<(unsigned)blocks, JP2_THREADS, 0, stream>>>(B, dq, naux, per_q, Jt);
+    }
 }
 
 // ---------------------------------------------------------------- tiles -> dense nbf x nbf
