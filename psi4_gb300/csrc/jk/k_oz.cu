@@ -65,7 +65,7 @@ constexpr int I8_BLOCK = NSL * I8_SLICE;     // 28 KB: all slices of one 128 x 3
 constexpr int E_EMPTY = -100000;             // exponent of an all-zero row
 constexpr int SMEM_BUDGET = 224 * 1024;
 constexpr int SMEM_RESERVE = 2048;
-constexpr int TR_THREADS = 448;              // producer, MMA, 8 epilogue warps, 4 converter warps
+constexpr int TR_THREADS = 480;              // producer, 2 MMA, 8 epilogue warps, 4 converter warps
 constexpr int CT_N = 64;                     // contraction tile columns
 constexpr int TR_MAX_N = 80;                 // half-transform accumulator columns
 constexpr int RUN_K = 1024;                  // contraction terms per accumulation run (levels 0-3 exact)
@@ -452,8 +452,11 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* v) {
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // one A slice (slot at TMEM column a_col) against the C^T slices of the stage: pairs (J, t),
-// t <= 6 - J, into accumulator min(J + t, 4); `first` starts a fresh accumulation run
-template <int NA, int J>
+// t <= 6 - J, into accumulator min(J + t, 4); `first` starts a fresh accumulation run.
+// PART 0 issues the pairs of the exact levels (accumulators 0..NA-2), PART 1 those of the tail
+// (accumulator NA-1): two threads issue them, each accumulator has one issuer, so the order of
+// the MMAs into an accumulator is the same as from a single issuer.
+template <int NA, int J, int PART>
 __device__ __forceinline__ void issue_slice(const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step, uint32_t id,
                                             bool first) {
 #pragma unroll
@@ -461,24 +464,26 @@ __device__ __forceinline__ void issue_slice(const uint32_t* d, uint32_t a_col, u
 #pragma unroll
         for (int t = 0; t <= NSL - 1 - J; ++t) {
             const int L = J + t < NA - 1 ? J + t : NA - 1;
+            if ((L < NA - 1) != (PART == 0)) continue;
             const uint32_t f = (first && ks == 0 && J == 0 && t <= NA - 1) ? 0u : 1u;
             mma_bf16_ta(d[L], a_col + (uint32_t)(8 * ks), dB + (uint64_t)t * b_step + (uint64_t)(2 * ks), id, f);
         }
     }
 }
 
-// slice j (0..6) of the A operand from its TMEM slot: the (7 - j) pairs with B slices 0..6-j
-template <int NA>
+// slice j (0..6) of the A operand from its TMEM slot: of the (7 - j) pairs with B slices
+// 0..6-j, those of issuer PART
+template <int NA, int PART>
 __device__ __forceinline__ void issue_slice_j(int j, const uint32_t* d, uint32_t a_col, uint64_t dB, uint64_t b_step,
                                               uint32_t id, bool first) {
     switch (j) {
-        case 0: issue_slice<NA, 0>(d, a_col, dB, b_step, id, first); break;
-        case 1: issue_slice<NA, 1>(d, a_col, dB, b_step, id, first); break;
-        case 2: issue_slice<NA, 2>(d, a_col, dB, b_step, id, first); break;
-        case 3: issue_slice<NA, 3>(d, a_col, dB, b_step, id, first); break;
-        case 4: issue_slice<NA, 4>(d, a_col, dB, b_step, id, first); break;
-        case 5: issue_slice<NA, 5>(d, a_col, dB, b_step, id, first); break;
-        default: issue_slice<NA, 6>(d, a_col, dB, b_step, id, first); break;
+        case 0: issue_slice<NA, 0, PART>(d, a_col, dB, b_step, id, first); break;
+        case 1: issue_slice<NA, 1, PART>(d, a_col, dB, b_step, id, first); break;
+        case 2: issue_slice<NA, 2, PART>(d, a_col, dB, b_step, id, first); break;
+        case 3: issue_slice<NA, 3, PART>(d, a_col, dB, b_step, id, first); break;
+        case 4: issue_slice<NA, 4, PART>(d, a_col, dB, b_step, id, first); break;
+        case 5: issue_slice<NA, 5, PART>(d, a_col, dB, b_step, id, first); break;
+        default: issue_slice<NA, 6, PART>(d, a_col, dB, b_step, id, first); break;
     }
 }
 
@@ -544,8 +549,10 @@ __device__ __forceinline__ void combine_n(const float* a, float& hi, float& lo) 
 
 // Persistent, warp-specialised: warp 0 lane 0 bulk-copies one k block (int8 A + BF16 C^T) per
 // stage; warps 6-9 convert A slice by slice into TMEM slots (each thread its own row);
-// warp 1 lane 0 issues the slice-pair MMAs; warps 2-5 drain the accumulators (tcgen05.ld)
-// after every run into double-float X and take the row maxima.
+// warp 1 lane 0 issues the slice-pair MMAs of the exact levels and warp 14 lane 0 those of the
+// tail (one thread issuing all 56 MMAs of a k block was the limit: ~89 cycles per MMA against
+// ~39 of tensor work); warps 2-5 and 10-13 drain the accumulators (tcgen05.ld) after every run
+// into double-float X and take the row maxima.
 __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -566,14 +573,14 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
     if (threadIdx.x == 0) {
         for (int s = 0; s < a.stages; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], 2);  // both MMA issuers commit
         }
         for (int r = 0; r < TR_ASLOTS; ++r) {
             tc::mbar_init(&afull[r], 128);
-            tc::mbar_init(&aempty[r], 1);
+            tc::mbar_init(&aempty[r], 2);
         }
         for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tfull[b], 2);
             tc::mbar_init(&tempty[b], 8);
         }
         *abort_flag = 0;
@@ -693,8 +700,11 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                 }
             }
         }
-    } else if (threadIdx.x == 32) {
-        // ---- MMA issuer: per k block, seven A slices from TMEM slots against one stage
+    } else if (threadIdx.x == 32 || threadIdx.x == 448) {
+        // ---- MMA issuers (warp 1: the exact levels' pairs, warp 14: the tail's): per k block,
+        // seven A slices from TMEM slots against one stage; both wait for every stage and A
+        // slot and both commit every release (the barriers count two arrivals)
+        const bool tail = threadIdx.x == 448;
         int s = 0, r = 0;
         uint32_t ph = 0, pr = 0;
         int ri = 0;
@@ -733,7 +743,10 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                         }
                         tc::tc_fence_after();
                         const uint32_t a_col = tmem + (uint32_t)(TR_ACOL0 + 16 * r);
-                        issue_slice_j<TR_NACC>(j, d, a_col, dB, b_step, id, first);
+                        if (tail)
+                            issue_slice_j<TR_NACC, 1>(j, d, a_col, dB, b_step, id, first);
+                        else
+                            issue_slice_j<TR_NACC, 0>(j, d, a_col, dB, b_step, id, first);
                         tc::mma_commit(&aempty[r]);
                         if (++r == TR_ASLOTS) {
                             r = 0;
@@ -750,7 +763,7 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                 tc::mma_commit(&tfull[buf]);
             }
         }
-    } else if (warp >= 2) {
+    } else if (warp >= 2 && warp < 14) {
         // ---- epilogue (warps 2-5 and 10-13, one column half each): after each run,
         // X (+)= run sum; after the last, the row maximum
         const int q = warp % 4;
