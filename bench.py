@@ -370,8 +370,9 @@ def run_gpu(args):
     roofline_j = {"bound": "hbm", "kernels": "j_pass1_kernel + j_pass2_kernel", "achieved": bytes_j / jt / 1e9,
                   "peak": hbm, "unit": "GB/s", "frac": bytes_j / jt / 1e9 / hbm,
                   "algorithmic_bytes_per_build": bytes_j, "j_only_ms": 1e3 * jt,
-                  "note": "of measured; timed on J-only builds (in a J+K build J runs on a second stream "
-                          "beside the K half-transform and joins before the contraction)"}
+                  "note": "of measured; timed on J-only builds (in a J+K build with a tensor-core K and at "
+                          "least 8 GB of B, J runs on a second stream beside the K kernels and joins at the "
+                          "end of the build)"}
 
     args._fp64_value = value / ws
     out = {"metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
