@@ -252,7 +252,7 @@ void join_j(gdfjk_t h) {
 }
 
 int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int nocc, int ldc, int mode, double* D_out,
-                  double* J, double* K, bool join = true) {
+                  double* J, double* K, bool join = true, bool reuse_C = false) {
     const bool do_J = mode & GDFJK_DO_J;
     const bool do_K = mode & GDFJK_DO_K;
     const bool nonsym = C_right != nullptr;
@@ -270,25 +270,29 @@ int enqueue_build(gdfjk_t h, const double* C_left, const double* C_right, int no
     cudaStream_t s = h->stream;
     TileLayout L = layout_of(h);
     CK(cudaEventRecord(h->ev[0], s));
-    // C (padded to nbf_pad x nocc_pad) and D = C_left C_right^T
-    if (nocc_pad > 0) {
+    // C padded to nbf_pad x nocc_pad (reuse_C: the previous build on this stream padded the
+    // same C into h->Cl, and nothing has written it since)
+    if (nocc_pad > 0 && !reuse_C) {
         launch_pad_C(C_left, h->nbf, nocc, ldc, h->nbf_pad, nocc_pad, h->Cl, s);
         if (nonsym) launch_pad_C(C_right, h->nbf, nocc, ldc, h->nbf_pad, nocc_pad, h->Cr, s);
     }
-    launch_density(h->Cl, nonsym ? h->Cr : h->Cl, h->nbf_pad, nocc_pad, h->D, s);
+    // D = C_left C_right^T (FP64, ~1 ms at nbf 1856): only J and the caller read it, no K path
+    // does.  It stays on K's stream ahead of the fork: on J's lowest-priority stream the K
+    // kernels starve it and J starts late (the mixed C2 build went from 42.8 to 49.0 ms)
+    if (do_J || D_out) launch_density(h->Cl, nonsym ? h->Cr : h->Cl, h->nbf_pad, nocc_pad, h->D, s);
     if (D_out) launch_copy_out(h->D, h->nbf, h->nbf_pad, D_out, s);
+    // J on the second stream only beside a tensor-core K (or alone, when the caller joins
+    // later) and only on a large B.  Measured on one GB300: at nbf 1856 / naux 4448 (61 GB of
+    // B) the emulated build went from 224 to 215 ms; at nbf 384 / naux 1856 (1.3 GB, J well
+    // under a millisecond) it went from 4.7 to 5.0 ms
+    const bool tc_k = !do_K || (mode & (GDFJK_MIXED | GDFJK_EMULATED));
+    const bool fork = do_J && tc_k && (double)h->naux * h->ntiles * 4096 * sizeof(double) >= J_FORK_MIN_BYTES;
+    cudaStream_t sj = fork ? h->stream_j : s;
+    if (fork) {
+        CK(cudaEventRecord(h->ev_fork, s));
+        CK(cudaStreamWaitEvent(sj, h->ev_fork, 0));
+    }
     if (do_J) {
-        // J on the second stream only beside a tensor-core K (or alone, when the caller joins
-        // later) and only on a large B.  Measured on one GB300: at nbf 1856 / naux 4448 (61 GB
-        // of B) the emulated build went from 224 to 215 ms; at nbf 384 / naux 1856 (1.3 GB,
-        // J well under a millisecond) it went from 4.7 to 5.0 ms
-        const bool tc_k = !do_K || (mode & (GDFJK_MIXED | GDFJK_EMULATED));
-        const bool fork = tc_k && (double)h->naux * h->ntiles * 4096 * sizeof(double) >= J_FORK_MIN_BYTES;
-        cudaStream_t sj = fork ? h->stream_j : s;
-        if (fork) {
-            CK(cudaEventRecord(h->ev_fork, s));
-            CK(cudaStreamWaitEvent(sj, h->ev_fork, 0));
-        }
         launch_weighted_density_tiles(h->D, h->nbf_pad, L, h->Dw, sj);
         launch_j_pass1(h->B, h->Dw, h->naux, L, h->dq, sj);
         launch_j_pass2(h->B, h->dq, h->naux, L, h->Jt, sj);
@@ -867,9 +871,10 @@ int enqueue_incremental(gdfjk_t h, const double* C, int nocc, int ldc, const dou
         }
     }
     if ((mode & GDFJK_DO_K) && !(mode & GDFJK_MIXED)) {
-        // FP64 anchor: a full FP64 K from C that becomes the base of later increments
+        // FP64 anchor: a full FP64 K from C that becomes the base of later increments (its C
+        // is the one the J build above padded: not padded again while J may still read it)
         rc = enqueue_build(h, nocc > 0 ? C : nullptr, nullptr, nocc, std::max(ldc, 1), GDFJK_DO_K | (mode & GDFJK_EMULATED),
-                           nullptr, nullptr, K);
+                           nullptr, nullptr, K, true, (mode & GDFJK_DO_J) != 0);
         if (rc) return rc;
         rc = mixed_set_base(h->mixed, K, h->nbf, s, h->err);
         if (rc) return rc;
