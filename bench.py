@@ -334,9 +334,10 @@ def run_gpu(args):
         issued = oz_issued_flops(nbf, naux, nocc)
         bf16_sus = float(peaks.get("bf16_tflops_sustained", 1696.1))
         bf16_burst = float(peaks.get("bf16_tflops", 1885.4))
-        # DRAM bytes of oz_transform_kernel from an ncu capture at naux 128 (3.72 GB per launch,
-        # profiles/oz_kernels_ncu.md), scaled by the aux functions processed
-        traffic = 3.72e9 * naux / 128.0 if (nbf, nocc) == (1856, 160) else None
+        # DRAM bytes of oz_transform_kernel from a single-kernel ncu capture of the same shape with
+        # 128 aux functions (3.291 GB read + 0.300 GB written per launch, 1.00x its algorithmic
+        # bytes), scaled by the aux functions processed: the traffic is linear in them
+        traffic = 3.591e9 * naux / 128.0 if (nbf, nocc) == (1856, 160) else None
         roofline = {"bound": "tensor", "kernel": "oz_transform_kernel", "achieved": issued / kt / 1e12,
                     "peak": bf16_sus, "unit": "TFLOP/s", "frac": issued / kt / 1e12 / bf16_sus, "traffic": traffic,
                     "traffic_note": "DRAM bytes per build, scaled from an ncu capture of the same kernel at naux 128 "
