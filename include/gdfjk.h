@@ -13,7 +13,10 @@
  * (GDFJK_OK = 0, negative on error) and gdfjk_last_error(h) gives the message (h may be
  * NULL for errors before a handle exists).  One CUDA stream per handle; calls that take
  * host buffers are synchronous, calls with the _device suffix are asynchronous on the
- * handle's stream.  A handle is not re-entrant (like psi4's JK objects, jk.h:232).
+ * handle's stream.  (A build may run its J passes on a second, internal stream beside the
+ * tensor-core K; that stream is joined back into the handle's stream before the build's
+ * last operation, so the handle's stream still orders everything a caller sees.)  A handle
+ * is not re-entrant (like psi4's JK objects, jk.h:232).
  */
 #ifndef GDFJK_H
 #define GDFJK_H
@@ -247,7 +250,9 @@ int gdfjk_trim(gdfjk_t h);
  * flags: mode bits of the forms in use, plus GDFJK_B_HOST (B then not counted). */
 int gdfjk_query_memory(int nbf, int naux, int max_nocc, int flags, size_t* bytes);
 
-/* Timing of the last build in milliseconds (J passes, K half-transform, K contraction). */
+/* Timing of the last build in milliseconds (J passes, K half-transform, K contraction).  When
+ * the J passes ran on the internal second stream beside K, j_ms is their span there, which
+ * then covers most of K's time rather than J's own. */
 int gdfjk_last_timings(gdfjk_t h, double* j_ms, double* k_transform_ms, double* k_contract_ms);
 
 /* Host watchdog: wait for the stream at most timeout_s seconds (GDFJK_ERR_TIMEOUT after). */
