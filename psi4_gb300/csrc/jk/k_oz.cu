@@ -403,6 +403,7 @@ struct TrArgs {
 // the tail is harmless here (no sums of squares; it is random relative to X).
 constexpr int TR_NACC = 5;
 constexpr int TR_ASLOTS = 7;  // a whole k block of A slices: the converters run one k block ahead
+static_assert(TR_ASLOTS == NSL, "slot r holds slice r of every k block (the slot pairs follow the slice pairs)");
 constexpr int TR_ACOL0 = 512 - TR_ASLOTS * 16;  // first A-slot column
 constexpr int TR_OFF_C = NSL * I8_SLICE;        // stage: [7 int8 A slices | 7 BF16 C^T slices]
 
@@ -657,7 +658,9 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                     const int nj = NSL - j0 < 2 ? NSL - j0 : 2;
                     int slot[2] = {0, 0};
                     for (int jj = 0; jj < nj; ++jj, ++used) {
-                        if (used >= TR_ASLOTS && !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
+                        // the issuers release a pair of slots with one commit on its last slot
+                        if (jj == nj - 1 && used >= TR_ASLOTS &&
+                            !tc::mbar_wait(&aempty[r], pr ^ 1u, abort_flag, a.err)) {
                             ok = false;
                             break;
                         }
@@ -692,7 +695,9 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                     }
                     tmem_wait_st();
                     tc::tc_fence_before();
-                    for (int jj = 0; jj < nj; ++jj) tc::mbar_arrive(&afull[slot[jj]]);
+                    // one arrival for the pair, on its last slot: every thread's stores to both
+                    // slots completed before it
+                    tc::mbar_arrive(&afull[nj == 2 ? slot[1] : slot[0]]);
                 }
                 if (++s == a.stages) {
                     s = 0;
@@ -737,17 +742,25 @@ __global__ void __launch_bounds__(TR_THREADS, 1) oz_transform_kernel(const TrArg
                     const bool first = kb == kb0;
 #pragma unroll
                     for (int j = 0; j < NSL; ++j) {
-                        if (!tc::mbar_wait(&afull[r], pr, abort_flag, a.err)) {
-                            ok = false;
-                            break;
+                        // the converters fill slots in pairs (j, j + 1) and arrive on the pair's
+                        // last slot only (each k block uses all seven slots, so r == j here):
+                        // one poll and one commit per pair
+                        const bool pair_first = (j & 1) == 0;
+                        const bool pair_last = (j & 1) == 1 || j == NSL - 1;
+                        if (pair_first) {
+                            const int rl = j + 1 < NSL ? r + 1 : r;
+                            if (!tc::mbar_wait(&afull[rl], pr, abort_flag, a.err)) {
+                                ok = false;
+                                break;
+                            }
+                            tc::tc_fence_after();
                         }
-                        tc::tc_fence_after();
                         const uint32_t a_col = tmem + (uint32_t)(TR_ACOL0 + 16 * r);
                         if (tail)
                             issue_slice_j<TR_NACC, 1>(j, d, a_col, dB, b_step, id, first);
                         else
                             issue_slice_j<TR_NACC, 0>(j, d, a_col, dB, b_step, id, first);
-                        tc::mma_commit(&aempty[r]);
+                        if (pair_last) tc::mma_commit(&aempty[r]);
                         if (++r == TR_ASLOTS) {
                             r = 0;
                             pr ^= 1u;
