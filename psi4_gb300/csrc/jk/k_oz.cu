@@ -36,8 +36,9 @@
 //                    one accumulation run per group, drained into a double-float running sum
 //                    in registers; split over groups; FP64 partials summed in a fixed order.
 // In both GEMMs one pipeline stage holds every digit slice of one 32-deep k block, and the
-// MMA issuer walks the A slices j = 0..6 (each from its TMEM slot) against B slices
-// t = 0..6-j, accumulator min(j + t, last).
+// MMA issuers walk the A slices j = 0..6 (in the half-transform each from its TMEM slot)
+// against B slices t = 0..6-j, accumulator min(j + t, last); the half-transform has two
+// issuing threads, one for the exact levels' accumulators and one for the tail's.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
