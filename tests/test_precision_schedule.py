@@ -52,7 +52,7 @@ def test_schedule_order_and_final_fp64_builds(ints_built):
     modes = [e["precision"] for e in res.log]
     assert len(modes) == res.iterations == len(jk.builds)
     assert [SETTINGS[m] for m in modes] == jk.builds
-    # increments first, at most one anchor, then FP64 rebuilds only
+    # increments first, one anchor, then FP64 rebuilds only
     assert modes[0] == "mixed"
     assert modes.count("anchor") == sched.n_anchor == 1  # water cc-pVDZ: m m m m m A m m m m F F
     first_fp64 = modes.index("fp64")
