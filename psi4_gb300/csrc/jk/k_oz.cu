@@ -1564,8 +1564,9 @@ int oz_build_K(OzState* o, const double* B, const TileLayout& L, const int* map_
         err = "emulated FP64: nocc above " + std::to_string(RUN_K) + " is not supported (use the native FP64 K)";
         return GDFJK_ERR_ARG;
     }
-    // ---- digits of C^T, in column chunks of <= 80 (six accumulators in the 512 TMEM columns,
-    // three pipeline stages in shared memory)
+    // ---- digits of C^T, in column chunks of <= 80 (five accumulators of N columns and seven
+    // 16-column A slots fill the 512 TMEM columns at N = 80; three pipeline stages in shared
+    // memory)
     const int nocc_p = nocc_pad;
     const int nchunk = (nocc_p + TR_MAX_N - 1) / TR_MAX_N;
     const int N = round_up((nocc_p + nchunk - 1) / nchunk, 16);
