@@ -133,8 +133,10 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 // ---------------------------------------------------------------- J pass 1: d_Q
 // One block per Q; the block streams B_Q (ntiles*4096 doubles, contiguous) once with
 // 16-byte loads, four independent partial sums per thread; Dw stays L2 resident.  Blocks are
-// small (256 threads, no dynamic shared memory) so that they fit beside a tensor-core K
-// kernel's CTA on the same SM: the J passes run on their own stream, concurrently with K.
+// small (256 threads, no dynamic shared memory) so that the J passes, on their own stream,
+// can run beside a tensor-core K kernel's CTA where the SM's registers allow: pass 2 (40
+// registers) fits beside both emulated-form K kernels, this pass (46, allocated as 48) does
+// not and runs in their gaps.
 constexpr int JP1_THREADS = 256;
 __global__ void __launch_bounds__(JP1_THREADS) j_pass1_kernel(const double* __restrict__ B,
                                                               const double* __restrict__ Dw, size_t per_q,
