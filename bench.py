@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -228,6 +229,34 @@ def cpu_baseline(nbf, naux, nocc, full_c4=True):
 OZ_PAIRS = 28  # BF16 slice-pair products per term of the emulated-FP64 form (7 digits, levels <= 6)
 
 
+def oz_aux_batches(nbf, naux, nocc, nonsym=False):
+    """Aux batches of one emulated-FP64 K build, by the engine's rule: multiples of the group
+    size G = 1024 // nocc_p aux functions whose double-float X and digit copies of X fit in
+    GDFJK_OZ_XCAP_GB (24 GB by default)."""
+    nbf_p = -(-nbf // 128) * 128
+    nocc_p = -(-nocc // 32) * 32
+    g = max(1, 1024 // nocc_p)
+    per_q = nocc_p * (nbf * 8.0 + (2.0 if nonsym else 1.0) * nbf_p * 7 * 2.0)
+    try:
+        cap_gb = float(os.environ.get("GDFJK_OZ_XCAP_GB", "24"))
+    except ValueError:
+        cap_gb = 24.0
+    if not cap_gb > 0.0:
+        cap_gb = 24.0
+    qb = max(1, int(min(naux, max(g, math.floor(cap_gb * 1e9 / per_q / g) * g))))
+    return -(-naux // qb)
+
+
+def build_launches(nbf, naux, nocc, emulated):
+    """Kernel launches of one lr-symmetric J+K build: J 6 (pad C, D, weighted D, two passes,
+    unpack); native K 4 (half-transform, contraction, reduction, unpack); emulated K 2 (column
+    exponents and digits of C) + 4 per aux batch (half-transform, split of X, contraction,
+    reduction)."""
+    if emulated:
+        return 6 + 2 + 4 * oz_aux_batches(nbf, naux, nocc)
+    return 10
+
+
 def oz_issued_flops(nbf, naux, nocc):
     """Issued BF16 tensor flops of the emulated-FP64 half-transform at padded sizes: 28 slice
     pairs x 2 x naux x nbf_p^2 x (column chunks of <= 80, multiples of 16)."""
@@ -389,7 +418,7 @@ def run_gpu(args):
            "e2e": e2e, "roofline": roofline, "roofline_j": roofline_j,
            "phase_ms": {"j": statistics.median(j_ms), "k_transform": statistics.median(kt_ms),
                         "k_contract": statistics.median(kc_ms)},
-           "clocks": clk, "gpu_launches": (12 if emulated else 10) * args.steps}
+           "clocks": clk, "gpu_launches": build_launches(nbf, naux, nocc, emulated) * args.steps}
 
     if emulated and rank == 0:
         # the native FP64 path at the same shape, for comparison
